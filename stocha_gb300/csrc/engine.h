@@ -1,0 +1,66 @@
+// Internal interface between the C-ABI host code (api.cpp) and the kernel
+// translation units.  Nothing here is exported from the shared library.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mc_types.h"
+
+namespace stocha {
+
+constexpr int kMaxAssets = 16;
+
+enum Model : int { kGbm = 0, kHeston = 1, kMerton = 2, kMultiGbm = 3 };
+enum Payoff : int { kCall = 0, kPut = 1 };
+
+// Model constants, computed on the host with the reference's expression order
+// so that every double the kernels start from equals the reference's.
+struct GbmK {  // gbm.rs:43-45
+  double s0, drift, diffusion;
+};
+struct HestonK {  // heston.rs:45-48 (Euler), :92-97,143-150 (QE)
+  double s0, v0, mu, kappa, theta, xi, rho;
+  double dt, sqrt_dt, rho_comp;
+  double e_kdt, k1, qe_m0, qe_s2b, one_m_ekdt;
+  double k0_s, k1_s, k2_s, k3_s, k4_s;
+  int scheme;  // 0 euler, 1 qe
+};
+struct MertonK {  // jump_diffusion.rs:49-64
+  double s0, drift, diffusion, mu_j, sigma_j;
+  uint64_t jump_thr;  // u < jump_prob  <=>  (u64 >> 11) < jump_thr
+};
+struct MultiK {  // multi_gbm.rs:22-40
+  int na;
+  double s0[kMaxAssets], drift[kMaxAssets], diffusion[kMaxAssets];
+  double L[kMaxAssets * kMaxAssets];  // lower Cholesky factor, row-major
+};
+
+// One launch of a path kernel over output rows [row_begin, row_begin+rows).
+struct PathLaunch {
+  StreamSpec ss;
+  const ZigTables* tabs;
+  unsigned* err;
+  // materialised mode: row-major rows of `row_len` values (out_f64 or out_f32)
+  double* out_f64;
+  float* out_f32;
+  int time_major;  // 1: out[step * rows + row] (internal consumers, e.g. LSMC)
+  // fused mode: per-block partial sums {sum payoff, sum payoff^2} per asset
+  double* partials;
+  double strike;
+  int payoff;
+  uint64_t row_begin, rows, steps, base_paths;
+  int model;
+  GbmK gbm;
+  HestonK heston;
+  MertonK merton;
+  MultiK multi;
+};
+
+// Launch helpers (paths_f64.cu / paths_f32.cu).  Return the number of blocks
+// launched (= number of partial records in fused mode), or -1 on error.
+int launch_paths_f64(const PathLaunch& L, cudaStream_t st);
+int launch_paths_f32(const PathLaunch& L, cudaStream_t st);
+// Sum per-block partials (deterministic order) into out[nvals].
+void launch_reduce_partials(const double* partials, int nblocks, int nvals, double* out, cudaStream_t st);
+
+}  // namespace stocha

@@ -1,0 +1,301 @@
+// FP64 path kernels: the reference's own discretisation of each model with
+// its exact operation order (this translation unit is built with
+// --fmad=false, so no a*b+c is contracted, as in Rust).  Each thread owns one
+// output row: it derives the row's stream by jump-ahead (gbm.rs:58-59) and
+// runs the model recurrence, either storing every step (materialised) or
+// reducing the terminal value to a call/put payoff in registers (fused).
+//
+//   GBM          src/finance/gbm.rs:42-107
+//   multi-GBM    src/finance/multi_gbm.rs:22-113
+//   Heston       src/finance/heston.rs:44-87 (Euler), :89-174 (QE)
+//   Merton       src/finance/jump_diffusion.rs:48-105
+#include <cuda_runtime.h>
+
+#include "engine.h"
+#include "mc_device.cuh"
+#include "reduce.cuh"
+
+namespace stocha {
+namespace {
+
+__device__ __forceinline__ double payoff_f64(double s, double k, int kind) {
+  return kind == kCall ? fmax(s - k, 0.0) : fmax(k - s, 0.0);
+}
+
+// Row-major (or time-major) store of one path value.
+__device__ __forceinline__ void store64(const PathLaunch& a, uint64_t lrow, uint64_t step, uint64_t width,
+                                        uint64_t col, double v) {
+  if (a.time_major)
+    a.out_f64[(step * width + col) * a.rows + lrow] = v;
+  else
+    a.out_f64[(lrow * (a.steps + 1) + step) * width + col] = v;
+}
+
+template <bool kStore>
+__global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  double acc = 0.0, acc2 = 0.0;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+    const uint64_t row = a.row_begin + lrow;
+    const bool neg = row >= a.base_paths;
+    PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
+    const double drift = a.gbm.drift, diffusion = a.gbm.diffusion;
+    double x = a.gbm.s0;
+    if (kStore) store64(a, lrow, 0, 1, 0, x);
+#pragma unroll 1
+    for (uint64_t k = 1; k <= a.steps; ++k) {
+      double z = normal_f64(s, c, zs, err);
+      if (neg) z = -z;
+      x *= exp(drift + diffusion * z);
+      if (kStore) store64(a, lrow, k, 1, 0, x);
+    }
+    if (!kStore) {
+      double p = payoff_f64(x, a.strike, a.payoff);
+      acc += p;
+      acc2 += p * p;
+    }
+  }
+  if (!kStore) block_sum2_store(acc, acc2, a.partials + 2 * blockIdx.x);
+  if (err) atomicOr(a.err, err);
+}
+
+template <int NA, bool kStore>
+__global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const int na = NA > 0 ? NA : a.multi.na;
+  unsigned err = 0;
+  double acc[NA > 0 ? NA : kMaxAssets], acc2[NA > 0 ? NA : kMaxAssets];
+  for (int i = 0; i < na; ++i) acc[i] = acc2[i] = 0.0;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+    const uint64_t row = a.row_begin + lrow;
+    const bool neg = row >= a.base_paths;
+    PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
+    double sv[NA > 0 ? NA : kMaxAssets], z[NA > 0 ? NA : kMaxAssets];
+#pragma unroll
+    for (int i = 0; i < na; ++i) {
+      sv[i] = a.multi.s0[i];
+      if (kStore) store64(a, lrow, 0, na, i, sv[i]);
+    }
+#pragma unroll 1
+    for (uint64_t k = 1; k <= a.steps; ++k) {
+#pragma unroll
+      for (int i = 0; i < na; ++i) z[i] = normal_f64(s, c, zs, err);
+      if (neg) {
+#pragma unroll
+        for (int i = 0; i < na; ++i) z[i] = -z[i];
+      }
+#pragma unroll
+      for (int i = 0; i < na; ++i) {
+        double eps = 0.0;
+#pragma unroll
+        for (int m = 0; m <= i; ++m) eps += a.multi.L[i * kMaxAssets + m] * z[m];
+        sv[i] *= exp(a.multi.drift[i] + a.multi.diffusion[i] * eps);
+        if (kStore) store64(a, lrow, k, na, i, sv[i]);
+      }
+    }
+    if (!kStore) {
+#pragma unroll
+      for (int i = 0; i < na; ++i) {
+        double p = payoff_f64(sv[i], a.strike, a.payoff);
+        acc[i] += p;
+        acc2[i] += p * p;
+      }
+    }
+  }
+  if (!kStore) {
+    for (int i = 0; i < na; ++i) block_sum2_store(acc[i], acc2[i], a.partials + (2 * (uint64_t)blockIdx.x) * na + 2 * i);
+  }
+  if (err) atomicOr(a.err, err);
+}
+
+// Rust powi for small non-negative exponents (compiler-rt __powidf2).
+__device__ __forceinline__ double powi_f64(double a, int b) {
+  double r = 1.0;
+  for (;;) {
+    if (b & 1) r *= a;
+    b /= 2;
+    if (b == 0) break;
+    a *= a;
+  }
+  return r;
+}
+
+template <bool kStore>
+__global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const HestonK& h = a.heston;
+  unsigned err = 0;
+  double acc = 0.0, acc2 = 0.0;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+    const uint64_t row = a.row_begin + lrow;
+    PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
+    double x = h.s0, v = h.v0;
+    if (kStore) store64(a, lrow, 0, 1, 0, x);
+    if (h.scheme == 0) {
+#pragma unroll 1
+      for (uint64_t k = 1; k <= a.steps; ++k) {
+        double dw1 = normal_f64(s, c, zs, err);
+        double dz = normal_f64(s, c, zs, err);
+        double dw2 = h.rho * dw1 + h.rho_comp * dz;
+        double v_plus = fmax(v, 0.0);
+        double sqrt_v = sqrt(v_plus);
+        v += h.kappa * (h.theta - v_plus) * h.dt + h.xi * sqrt_v * h.sqrt_dt * dw2;
+        x *= exp((h.mu - 0.5 * v_plus) * h.dt + sqrt_v * h.sqrt_dt * dw1);
+        if (kStore) store64(a, lrow, k, 1, 0, x);
+      }
+    } else {
+#pragma unroll 1
+      for (uint64_t k = 1; k <= a.steps; ++k) {
+        double v_plus = fmax(v, 0.0);
+        double m = h.qe_m0 + v_plus * h.e_kdt;
+        m = fmax(m, 1e-15);
+        double s2 = v_plus * h.xi * h.xi * h.e_kdt * h.one_m_ekdt / h.kappa + h.qe_s2b;
+        double psi = s2 / (m * m);
+        double v_next;
+        if (psi <= 1.5) {
+          double b2 = 2.0 / psi - 1.0 + sqrt(2.0 / psi * (2.0 / psi - 1.0));
+          b2 = fmax(b2, 0.0);
+          double aa = m / (1.0 + b2);
+          double b = sqrt(b2);
+          double z = normal_f64(s, c, zs, err);
+          v_next = aa * (b + z) * (b + z);
+        } else {
+          double p = (psi - 1.0) / (psi + 1.0);
+          double beta = (1.0 - p) / m;
+          double u = u64_to_unit_f64(s.next());
+          v_next = (u <= p) ? 0.0 : log((1.0 - p) / (1.0 - u)) / beta;
+        }
+        v_next = fmax(v_next, 0.0);
+        double z1 = normal_f64(s, c, zs, err);
+        double var_term = fmax(h.k3_s * v_plus + h.k4_s * v_next, 0.0);
+        double log_s = log(x) + h.k0_s + h.k1_s * v_plus + h.k2_s * v_next + sqrt(var_term) * z1;
+        x = exp(fmin(fmax(log_s, -500.0), 500.0));
+        v = v_next;
+        if (kStore) store64(a, lrow, k, 1, 0, x);
+      }
+    }
+    if (!kStore) {
+      double p = payoff_f64(x, a.strike, a.payoff);
+      acc += p;
+      acc2 += p * p;
+    }
+  }
+  if (!kStore) block_sum2_store(acc, acc2, a.partials + 2 * blockIdx.x);
+  if (err) atomicOr(a.err, err);
+}
+
+template <bool kStore>
+__global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const MertonK& M = a.merton;
+  unsigned err = 0;
+  double acc = 0.0, acc2 = 0.0;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+    const uint64_t row = a.row_begin + lrow;
+    PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
+    double x = M.s0;
+    if (kStore) store64(a, lrow, 0, 1, 0, x);
+#pragma unroll 1
+    for (uint64_t k = 1; k <= a.steps; ++k) {
+      double z = normal_f64(s, c, zs, err);
+      double diffusion_return = M.drift + M.diffusion * z;
+      uint64_t u = s.next();
+      double jump_return = 0.0;
+      if ((u >> 11) < M.jump_thr) {
+        double z_j = normal_f64(s, c, zs, err);
+        jump_return = M.mu_j + M.sigma_j * z_j;
+      }
+      x *= exp(diffusion_return + jump_return);
+      if (kStore) store64(a, lrow, k, 1, 0, x);
+    }
+    if (!kStore) {
+      double p = payoff_f64(x, a.strike, a.payoff);
+      acc += p;
+      acc2 += p * p;
+    }
+  }
+  if (!kStore) block_sum2_store(acc, acc2, a.partials + 2 * blockIdx.x);
+  if (err) atomicOr(a.err, err);
+}
+
+__global__ void k_reduce_partials(const double* __restrict__ partials, int nblocks, int nvals,
+                                  double* __restrict__ out) {
+  // one block; thread t owns value t; fixed summation order -> deterministic
+  for (int v = threadIdx.x; v < nvals; v += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partials[(uint64_t)b * nvals + v];
+    out[v] = s;
+  }
+}
+
+template <bool kStore>
+int launch_multi(const PathLaunch& L, dim3 g, dim3 b, cudaStream_t st) {
+  switch (L.multi.na) {
+    case 1: k_multi_gbm_f64<1, kStore><<<g, b, 0, st>>>(L); break;
+    case 2: k_multi_gbm_f64<2, kStore><<<g, b, 0, st>>>(L); break;
+    case 3: k_multi_gbm_f64<3, kStore><<<g, b, 0, st>>>(L); break;
+    case 4: k_multi_gbm_f64<4, kStore><<<g, b, 0, st>>>(L); break;
+    default: k_multi_gbm_f64<0, kStore><<<g, b, 0, st>>>(L); break;
+  }
+  return 0;
+}
+
+}  // namespace
+
+// Grid: one thread per row when that fits the GPU; small row counts use
+// single-warp blocks so every SM gets an equal share of warps.
+static void pick_grid(uint64_t rows, int* grid, int* block) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int b = rows <= (uint64_t)sms * 1024 ? 32 : 128;
+  uint64_t g = (rows + b - 1) / b;
+  uint64_t cap = (uint64_t)sms * 64;  // grid-stride beyond this
+  if (g > cap) g = cap;
+  if (g < 1) g = 1;
+  *grid = (int)g;
+  *block = b;
+}
+
+int launch_paths_f64(const PathLaunch& L, cudaStream_t st) {
+  int g, b;
+  pick_grid(L.rows, &g, &b);
+  const bool store = L.out_f64 != nullptr;
+  dim3 G(g), B(b);
+  switch (L.model) {
+    case kGbm:
+      if (store) k_gbm_f64<true><<<G, B, 0, st>>>(L); else k_gbm_f64<false><<<G, B, 0, st>>>(L);
+      break;
+    case kHeston:
+      if (store) k_heston_f64<true><<<G, B, 0, st>>>(L); else k_heston_f64<false><<<G, B, 0, st>>>(L);
+      break;
+    case kMerton:
+      if (store) k_merton_f64<true><<<G, B, 0, st>>>(L); else k_merton_f64<false><<<G, B, 0, st>>>(L);
+      break;
+    case kMultiGbm:
+      if (store) launch_multi<true>(L, G, B, st); else launch_multi<false>(L, G, B, st);
+      break;
+    default:
+      return -1;
+  }
+  return cudaPeekAtLastError() == cudaSuccess ? g : -1;
+}
+
+void launch_reduce_partials(const double* partials, int nblocks, int nvals, double* out, cudaStream_t st) {
+  k_reduce_partials<<<1, 64, 0, st>>>(partials, nblocks, nvals, out);
+}
+
+}  // namespace stocha

@@ -1,0 +1,295 @@
+// Host side of the RNG surface (src/lib.rs:74-184, src/prng/pcg64.rs): state
+// bookkeeping, JSON state files, and the launches of rng.cu.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "host_common.h"
+#include "rng_kernels.h"
+
+using namespace stocha;
+
+namespace {
+
+u128 rng_state(const stocha_rng* r) { return ((u128)r->state_hi << 64) | r->state_lo; }
+u128 rng_inc(const stocha_rng* r) { return ((u128)r->inc_hi << 64) | r->inc_lo; }
+void set_state(stocha_rng* r, u128 s) {
+  r->state_lo = (uint64_t)s;
+  r->state_hi = (uint64_t)(s >> 64);
+}
+
+PcgJump affine_jump(u128 inc, u128 delta) {
+  u128 st = 0;
+  // A*0 + C = C; A from advancing the state 1 by delta minus C.
+  u128 one = 1;
+  u128 c = st;
+  pcg_advance(&c, inc, delta);  // c = C
+  u128 a = one;
+  pcg_advance(&a, inc, delta);  // a = A + C
+  a -= c;
+  PcgJump J;
+  J.mul_lo = (uint64_t)a;
+  J.mul_hi = (uint64_t)(a >> 64);
+  J.add_lo = (uint64_t)c;
+  J.add_hi = (uint64_t)(c >> 64);
+  return J;
+}
+
+int device_count_threads(int device) {
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  return sms * 1024;
+}
+
+// raw (kind 0) or uniform (kind 1) draws into host memory
+int fill_raw(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, void* out) {
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  if (n == 0) return STOCHA_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const uint64_t bytes = n * 8;
+  if ((rc = ensure_buf(ctx, ctx->out, bytes))) return rc;
+  uint64_t threads = (uint64_t)device_count_threads(ctx->device);
+  if (threads > n) threads = n;
+  StreamSpec ss;
+  make_stream_spec_state(rng_state(r), rng_inc(r), 1, &ss);
+  PcgJump stride = affine_jump(rng_inc(r), threads);
+  if ((rc = begin_call(ctx))) return rc;
+  launch_rng_raw(ss, stride, threads, n, kind, ctx->out.ptr, ctx->stream);
+  STOCHA_CUDA(cudaGetLastError());
+  STOCHA_CUDA(cudaMemcpyAsync(out, ctx->out.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if ((rc = finish_call(ctx))) return rc;
+  u128 s = rng_state(r);
+  pcg_advance(&s, rng_inc(r), n);
+  set_state(r, s);
+  return STOCHA_OK;
+}
+
+int fill_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, double loc, double scale, double* out) {
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  if (n == 0) return STOCHA_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  const uint32_t C = kRngChunk;
+  // expected 1.0296 draws per normal; generous margin, doubled on shortfall
+  double need = (double)n * 1.04 + 16.0 * std::sqrt((double)n) + 2.0 * C;
+  uint64_t nchunks = (uint64_t)(need / C) + 2;
+  StreamSpec ss;
+  make_stream_spec_state(rng_state(r), rng_inc(r), 1, &ss);
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    const size_t off_counts = 0;
+    const size_t off_exits = off_counts + nchunks * kRngEntries * 4;
+    const size_t off_entry = off_exits + nchunks * kRngEntries * 4;
+    const size_t off_cnt = off_entry + nchunks * 4;
+    const size_t off_offset = ((off_cnt + nchunks * 4) + 7) & ~(size_t)7;
+    const size_t off_total = off_offset + nchunks * 8;
+    const size_t aux_bytes = off_total + 16;
+    if ((rc = ensure_buf(ctx, ctx->aux, aux_bytes))) return rc;
+    if ((rc = ensure_buf(ctx, ctx->out, n * 8))) return rc;
+    char* aux = (char*)ctx->aux.ptr;
+    uint32_t* counts = (uint32_t*)(aux + off_counts);
+    uint32_t* exits = (uint32_t*)(aux + off_exits);
+    uint32_t* entry = (uint32_t*)(aux + off_entry);
+    uint32_t* cnt = (uint32_t*)(aux + off_cnt);
+    uint64_t* offset = (uint64_t*)(aux + off_offset);
+    uint64_t* total = (uint64_t*)(aux + off_total);
+    uint64_t* final_pos = total + 1;
+    if ((rc = begin_call(ctx))) return rc;
+    launch_rng_parse(ss, ctx->d_tabs, nchunks, C, counts, exits, entry, cnt, offset, total, ctx->d_err, ctx->stream);
+    STOCHA_CUDA(cudaGetLastError());
+    STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, total, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = finish_call(ctx))) return rc;
+    uint64_t got;
+    std::memcpy(&got, ctx->h_small, 8);
+    if (got < n) {
+      nchunks = nchunks * 3 / 2 + 2;
+      continue;
+    }
+    if ((rc = begin_call(ctx))) return rc;
+    launch_rng_emit(ss, ctx->d_tabs, nchunks, C, entry, cnt, offset, n, kind, loc, scale, (double*)ctx->out.ptr,
+                    final_pos, ctx->d_err, ctx->stream);
+    STOCHA_CUDA(cudaGetLastError());
+    STOCHA_CUDA(cudaMemcpyAsync(out, ctx->out.ptr, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, final_pos, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = finish_call(ctx))) return rc;
+    uint64_t fp;
+    std::memcpy(&fp, ctx->h_small, 8);
+    u128 s = rng_state(r);
+    pcg_advance(&s, rng_inc(r), fp);
+    set_state(r, s);
+    return STOCHA_OK;
+  }
+  return set_error(STOCHA_ERR_DEVICE, "normal stream parse did not cover the request");
+}
+
+// ---- minimal JSON reader for the state files of pcg64.rs:10-20 ----------
+struct Json {
+  const char* p;
+  const char* end;
+  bool ok = true;
+
+  void ws() {
+    while (p < end && (*p == ' ' || *p == '\n' || *p == '\t' || *p == '\r')) ++p;
+  }
+  bool eat(char c) {
+    ws();
+    if (p < end && *p == c) {
+      ++p;
+      return true;
+    }
+    return false;
+  }
+  // value kinds: 0 other, 1 unsigned integer (fits u128), 2 object
+  struct Val {
+    int kind = 0;
+    u128 u = 0;
+    std::vector<std::pair<std::string, Val>> obj;
+  };
+  bool str(std::string* s) {
+    ws();
+    if (p >= end || *p != '"') return false;
+    ++p;
+    while (p < end && *p != '"') {
+      if (*p == '\\') {
+        ++p;
+        if (p >= end) return false;
+      }
+      s->push_back(*p++);
+    }
+    if (p >= end) return false;
+    ++p;
+    return true;
+  }
+  bool value(Val* v, int depth) {
+    ws();
+    if (p >= end || depth > 32) return false;
+    if (*p == '{') {
+      ++p;
+      v->kind = 2;
+      if (eat('}')) return true;
+      for (;;) {
+        std::string k;
+        if (!str(&k) || !eat(':')) return false;
+        Val c;
+        if (!value(&c, depth + 1)) return false;
+        v->obj.emplace_back(k, c);
+        if (eat(',')) continue;
+        return eat('}');
+      }
+    }
+    if (*p == '[') {
+      ++p;
+      if (eat(']')) return true;
+      for (;;) {
+        Val c;
+        if (!value(&c, depth + 1)) return false;
+        if (eat(',')) continue;
+        return eat(']');
+      }
+    }
+    if (*p == '"') {
+      std::string s;
+      return str(&s);
+    }
+    if (*p >= '0' && *p <= '9') {
+      const char* q = p;
+      u128 acc = 0;
+      bool overflow = false;
+      while (p < end && *p >= '0' && *p <= '9') {
+        u128 nxt = acc * 10 + (u128)(*p - '0');
+        if (nxt / 10 != acc) overflow = true;
+        acc = nxt;
+        ++p;
+      }
+      bool integral = !(p < end && (*p == '.' || *p == 'e' || *p == 'E'));
+      while (p < end && (*p == '.' || *p == 'e' || *p == 'E' || *p == '+' || *p == '-' || (*p >= '0' && *p <= '9')))
+        ++p;
+      if (integral && !overflow && !(p - q > 1 && *q == '0')) {
+        v->kind = 1;
+        v->u = acc;
+      }
+      return true;
+    }
+    if (*p == '-') {
+      ++p;
+      while (p < end && (*p == '.' || *p == 'e' || *p == 'E' || *p == '+' || *p == '-' || (*p >= '0' && *p <= '9')))
+        ++p;
+      return true;
+    }
+    for (const char* lit : {"true", "false", "null"}) {
+      size_t L = std::strlen(lit);
+      if ((size_t)(end - p) >= L && std::strncmp(p, lit, L) == 0) {
+        p += L;
+        return true;
+      }
+    }
+    return false;
+  }
+};
+
+const Json::Val* field(const Json::Val& o, const char* k) {
+  const Json::Val* hit = nullptr;
+  for (auto& kv : o.obj)
+    if (kv.first == k) hit = &kv.second;
+  return hit;
+}
+
+}  // namespace
+
+extern "C" {
+
+int stocha_rng_uniform(stocha_ctx* ctx, stocha_rng* r, uint64_t size, double* out) {
+  return fill_raw(ctx, r, size, 1, out);
+}
+
+int stocha_rng_raw_u64(stocha_ctx* ctx, stocha_rng* r, uint64_t size, uint64_t* out) {
+  return fill_raw(ctx, r, size, 0, out);
+}
+
+int stocha_rng_standard_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t size, double* out) {
+  return fill_normal(ctx, r, size, 1, 0.0, 1.0, out);
+}
+
+int stocha_rng_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t size, double loc, double scale, double* out) {
+  if (scale <= 0.0) return set_error(STOCHA_ERR_VALUE, "scale must be positive");  // lib.rs:137-141
+  return fill_normal(ctx, r, size, 2, loc, scale, out);
+}
+
+// pcg64.rs:68-77: the full state {"version", "rng": {"state", "increment"},
+// "seed"} restores the exact position; {"seed": N} restarts the stream.
+int stocha_rng_from_state(const char* json, stocha_rng* out) {
+  if (!json) return set_error(STOCHA_ERR_VALUE, "invalid state JSON");
+  Json J{json, json + std::strlen(json)};
+  Json::Val root;
+  bool parsed = J.value(&root, 0);
+  J.ws();
+  if (!parsed || J.p != J.end) {
+    size_t col = (size_t)(J.p - json) + 1;
+    return set_error(STOCHA_ERR_VALUE, "invalid state JSON at line 1 column " + std::to_string(col));
+  }
+  if (root.kind == 2) {
+    const Json::Val* ver = field(root, "version");
+    const Json::Val* rng = field(root, "rng");
+    const Json::Val* seed = field(root, "seed");
+    if (ver && ver->kind == 1 && ver->u <= 255 && rng && rng->kind == 2 && seed && seed->kind == 1) {
+      const Json::Val* st = field(*rng, "state");
+      const Json::Val* inc = field(*rng, "increment");
+      if (st && st->kind == 1 && inc && inc->kind == 1) {
+        set_state(out, st->u);
+        out->inc_lo = (uint64_t)inc->u;
+        out->inc_hi = (uint64_t)(inc->u >> 64);
+        out->seed_lo = (uint64_t)seed->u;
+        out->seed_hi = (uint64_t)(seed->u >> 64);
+        return STOCHA_OK;
+      }
+    }
+    if (seed && seed->kind == 1) return stocha_rng_new((uint64_t)seed->u, (uint64_t)(seed->u >> 64), nullptr, out);
+    return set_error(STOCHA_ERR_VALUE, "missing field `seed`");
+  }
+  return set_error(STOCHA_ERR_VALUE, "invalid type: expected struct SeedOnly");
+}
+
+}  // extern "C"

@@ -1,0 +1,22 @@
+// Launchers of the RNG-surface kernels (rng.cu), used by rng_host.cpp.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mc_types.h"
+
+namespace stocha {
+
+constexpr int kRngEntries = 4;        // candidate entry offsets parsed per chunk
+constexpr uint32_t kRngChunk = 512;   // draws per chunk
+
+void launch_rng_raw(const StreamSpec& ss, const PcgJump& stride, uint64_t threads, uint64_t n, int kind,
+                    void* out, cudaStream_t st);
+void launch_rng_parse(const StreamSpec& ss, const ZigTables* tabs, uint64_t nchunks, uint32_t C, uint32_t* counts,
+                      uint32_t* exits, uint32_t* entry, uint32_t* cnt, uint64_t* offset, uint64_t* total,
+                      unsigned* err, cudaStream_t st);
+void launch_rng_emit(const StreamSpec& ss, const ZigTables* tabs, uint64_t nchunks, uint32_t C,
+                     const uint32_t* entry, const uint32_t* cnt, const uint64_t* offset, uint64_t n, int kind,
+                     double loc, double scale, double* out, uint64_t* final_pos, unsigned* err, cudaStream_t st);
+
+}  // namespace stocha

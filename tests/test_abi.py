@@ -1,0 +1,125 @@
+"""The C ABI and host logic, without a GPU.
+
+* libstocha_gpu.so builds (nvcc cross-compiles for sm_103a) and exports every
+  function include/stocha_gpu.h declares.
+* Argument validation happens on the host before any CUDA call and raises the
+  reference's exceptions and messages (src/lib.rs), checked here the way the
+  reference's own tests check them.
+* The integer fast-path thresholds equal the reference's FP64 comparison.
+"""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _declared():
+    src = open(os.path.join(ROOT, "include", "stocha_gpu.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(stocha_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol(stocha):
+    from stocha_gb300 import _lib
+
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    names = _declared()
+    assert len(names) >= 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_fast_path_thresholds_match_fp64_compare(stocha):
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    thr = np.zeros(256, np.uint64)
+    lib.stocha_debug_zig_thresholds.argtypes = [_lib.P_u64]
+    assert lib.stocha_debug_zig_thresholds(thr.ctypes.data_as(_lib.P_u64)) == 0
+    from tests.test_oracle import _table_from_inc
+
+    _, X, _ = _table_from_inc()
+    rng = np.random.default_rng(5)
+    two53 = 2.0**-53
+    for L in range(256):
+        t = int(thr[L])
+        cands = [0, 1, t - 2, t - 1, t, t + 1, 2**53 - 1] + [int(v) for v in rng.integers(0, 2**53, 64)]
+        for m in cands:
+            if 0 <= m < 2**53:
+                fast = (float(m) * two53) * X[L] < X[L + 1]  # normal.rs:25-27
+                assert fast == (m < t), (L, m, t)
+    assert int(thr[255]) == 0  # X[256] = 0: layer 255 never takes the fast path
+
+
+def test_validation_messages(stocha):
+    s = stocha
+    cases = [
+        (lambda: s.gbm(-1.0, 0.05, 0.2, 1.0, 10, 10), "s0 must be positive"),
+        (lambda: s.gbm(100.0, 0.05, 0.0, 1.0, 10, 5), "sigma must be positive"),
+        (lambda: s.gbm(100.0, 0.05, 0.2, -1.0, 10, 10), "t must be positive"),
+        (lambda: s.gbm(100.0, 0.05, 0.2, 1.0, 0, 10), "steps and n_paths must be positive"),
+        (lambda: s.heston(100, -0.1, 0.05, 2, 0.04, 0.3, -0.7, 1, 10, 10), "v0 must be non-negative"),
+        (lambda: s.heston(100, 0.04, 0.05, 0, 0.04, 0.3, -0.7, 1, 10, 10), "kappa must be positive"),
+        (lambda: s.heston(100, 0.04, 0.05, 2, 0, 0.3, -0.7, 1, 10, 10), "theta must be positive"),
+        (lambda: s.heston(100, 0.04, 0.05, 2, 0.04, 0, -0.7, 1, 10, 10), "xi must be positive"),
+        (lambda: s.heston(100, 0.04, 0.05, 2, 0.04, 0.3, 2.0, 1, 10, 10), "rho must be in [-1, 1]"),
+        (lambda: s.heston(100, 0.04, 0.05, 2, 0.04, 0.3, -0.7, 1, 10, 10, scheme="bad"),
+         "scheme must be 'euler' or 'qe'"),
+        (lambda: s.merton_jump_diffusion(100, 0.05, 0.0, 1, -0.05, 0.1, 1, 10, 10), "sigma must be positive"),
+        (lambda: s.merton_jump_diffusion(100, 0.05, 0.2, -1, -0.05, 0.1, 1, 10, 10), "lambda_ must be non-negative"),
+        (lambda: s.merton_jump_diffusion(100, 0.05, 0.2, 1, -0.05, -0.1, 1, 10, 10), "sigma_j must be non-negative"),
+        (lambda: s.multi_gbm([], [], [], np.eye(1), 1.0, 10, 10), "s0 must not be empty"),
+        (lambda: s.multi_gbm([100.0], [0.05, 0.08], [0.2], np.eye(1), 1.0, 10, 10),
+         "s0, mu, sigma must have the same length"),
+        (lambda: s.multi_gbm([-1.0, 50.0], [0.05, 0.08], [0.2, 0.3], np.eye(2), 1.0, 10, 10),
+         "all s0 must be positive"),
+        (lambda: s.multi_gbm([100.0, 50.0], [0.05, 0.08], [0.2, 0.0], np.eye(2), 1.0, 10, 10),
+         "all sigma must be positive"),
+        (lambda: s.multi_gbm([100.0, 50.0], [0.05, 0.08], [0.2, 0.3], np.eye(3), 1.0, 10, 10),
+         "corr must be (2, 2), got (3, 3)"),
+        (lambda: s.multi_gbm([100.0, 50.0], [0.05, 0.08], [0.2, 0.3], np.array([[1.0, 1.5], [1.5, 1.0]]), 1.0,
+                             10, 10), "matrix is not positive-definite (diagonal element 1 = -1.25)"),
+        (lambda: s.RNG(seed=0).normal(size=10, scale=-1.0), "scale must be positive"),
+        (lambda: s.RNG(seed=0, algorithm="mt"), "Unknown algorithm: 'mt'. Supported: 'pcg64dxsm'"),
+    ]
+    for fn, msg in cases:
+        with pytest.raises(ValueError) as ei:
+            fn()
+        assert str(ei.value) == msg
+
+
+def test_conversion_errors(stocha):
+    with pytest.raises(OverflowError):
+        stocha.gbm(100.0, 0.05, 0.2, 1.0, -5, 10)
+    with pytest.raises(OverflowError):
+        stocha.gbm(100.0, 0.05, 0.2, 1.0, 10, 10, seed=2**64)
+    with pytest.raises(TypeError):
+        stocha.gbm(100.0, 0.05, 0.2, 1.0, 10.5, 10)
+    with pytest.raises(OverflowError):
+        stocha.RNG(seed=2**128)
+
+
+def test_rng_state_json_roundtrip(stocha):
+    r = stocha.RNG(seed=2**100 + 7)
+    assert r.seed == 2**100 + 7 and repr(r) == f"RNG(seed={2**100 + 7}, algorithm='pcg64dxsm')"
+    js = r.save_state()
+    assert js.startswith('{"version":2,"rng":{"state":') and js.endswith(f',"seed":{2**100 + 7}}}')
+    r2 = stocha.RNG.from_state(js)
+    assert r2.save_state() == js and r2.seed == r.seed
+    legacy = stocha.RNG.from_state('{"seed":42}')
+    assert legacy.save_state() == stocha.RNG(seed=42).save_state()
+    with pytest.raises(ValueError):
+        stocha.RNG.from_state("not-valid-json")
+
+
+def test_rng_seed_state_matches_oracle(stocha, oracle):
+    for seed in (0, 42, 2**64 + 3, 2**128 - 1):
+        r = stocha.RNG(seed=seed)
+        st, inc = oracle.pcg_seed(seed)
+        js = r.save_state()
+        assert f'"state":{st},' in js and f'"increment":{inc}}}' in js

@@ -1,0 +1,162 @@
+"""Device paths and draws against the CPU oracle (FP64 plain form).
+
+Bars (the engine's parity contract):
+  * RNG integers, uniforms and normals of the RNG surface: bit-exact.
+  * FP64 paths: within PATH_RTOL relative of the oracle; column 0 exact.
+    (The only non-basic operation on the path is exp(): CUDA's and glibc's
+    differ by at most an ulp now and then, compounded over <= 252 steps.)
+  * Full-size runs: rows are a function of their own index only, so the first
+    rows of a 1e6-path run must equal an oracle run of those rows.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PATH_RTOL = 1e-12
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))) if a.size else 0.0
+
+
+# ------------------------------------------------------------------- RNG ---
+@pytest.mark.parametrize("seed", [0, 42, 2**64 + 3, 2**128 - 1])
+def test_raw_u64_bit_exact(stocha, oracle, seed):
+    r = stocha._stocha.RNG(seed=seed)
+    st, inc = oracle.pcg_seed(seed)
+    a = r.raw_u64(1)
+    b = r.raw_u64(1_000_003)
+    want = oracle.pcg_u64(st, inc, 1_000_004)
+    np.testing.assert_array_equal(np.concatenate([a, b]), want)
+
+
+def test_uniform_bit_exact_and_continuous(stocha, oracle):
+    r = stocha.RNG(seed=7)
+    st, inc = oracle.pcg_seed(7)
+    got = np.concatenate([r.uniform(100), r.uniform(12345), r.uniform(1)])
+    want, _, _ = oracle.stream_fill(st, inc, "uniform", 100 + 12345 + 1)
+    np.testing.assert_array_equal(got, want)
+    assert got.min() >= 0.0 and got.max() < 1.0
+
+
+@pytest.mark.parametrize("sizes", [[1], [7, 1000], [100_003], [1_000_000, 5]])
+def test_standard_normal_bit_exact(stocha, oracle, sizes):
+    r = stocha.RNG(seed=123)
+    st, inc = oracle.pcg_seed(123)
+    got = np.concatenate([r.standard_normal(n) for n in sizes])
+    want, used, st_end = oracle.stream_fill(st, inc, "standard_normal", sum(sizes))
+    np.testing.assert_array_equal(got, want)
+    # the generator position after the calls is the reference's
+    assert f'"state":{st_end},' in r.save_state()
+
+
+def test_normal_loc_scale_and_state_roundtrip(stocha, oracle):
+    r = stocha.RNG(seed=42)
+    _ = r.normal(size=500)
+    js = r.save_state()
+    expected = r.normal(size=100, loc=5.0, scale=2.0)
+    restored = stocha.RNG.from_state(js)
+    np.testing.assert_array_equal(restored.normal(size=100, loc=5.0, scale=2.0), expected)
+    st, inc = oracle.pcg_seed(42)
+    _, _, st2 = oracle.stream_fill(st, inc, "standard_normal", 500)
+    want, _, _ = oracle.stream_fill(st2, inc, "normal", 100, loc=5.0, scale=2.0)
+    np.testing.assert_array_equal(expected, want)
+
+
+def test_empty_draws(stocha):
+    r = stocha.RNG(seed=1)
+    js = r.save_state()
+    assert r.standard_normal(0).shape == (0,) and r.uniform(0).shape == (0,)
+    assert r.save_state() == js
+
+
+# ----------------------------------------------------------------- paths ---
+GBM_CASES = [
+    dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=252, n_paths=2000, seed=42),
+    dict(s0=50.0, mu=0.0, sigma=0.1, t=1.0, steps=10, n_paths=100, seed=0),
+    dict(s0=100.0, mu=0.08, sigma=0.2, t=1.0, steps=52, n_paths=1001, seed=7, q=0.03),
+    dict(s0=100.0, mu=0.05, sigma=0.9, t=3.0, steps=1, n_paths=333, seed=2**63 + 11),
+    dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=252, n_paths=1001, seed=42, antithetic=True),
+    dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=3, n_paths=1, seed=5, antithetic=True),
+]
+
+
+@pytest.mark.parametrize("kw", GBM_CASES)
+def test_gbm_parity(stocha, oracle, kw):
+    got = stocha.gbm(**kw)
+    want = oracle.gbm(kw["s0"], kw["mu"], kw["sigma"], kw["t"], kw["steps"], kw["n_paths"], seed=kw["seed"],
+                      antithetic=kw.get("antithetic", False), q=kw.get("q", 0.0))
+    assert got.shape == want.shape and got.dtype == np.float64 and got.flags.c_contiguous
+    np.testing.assert_array_equal(got[:, 0], kw["s0"])
+    assert _rel(got, want) <= PATH_RTOL
+
+
+def test_gbm_config1_full_size(stocha, oracle):
+    """s0=100, mu=0.05, sigma=0.20, t=1, steps=252, n_paths=100000, seed=42."""
+    got = stocha.gbm(100.0, 0.05, 0.2, 1.0, 252, 100_000, seed=42)
+    want = oracle.gbm(100.0, 0.05, 0.2, 1.0, 252, 100_000, seed=42)
+    assert got.shape == (100_000, 253)
+    assert _rel(got, want) <= PATH_RTOL
+    assert abs(got[:, -1].mean() / (100 * math.exp(0.05)) - 1) < 5e-3
+
+
+@pytest.mark.parametrize("na,anti", [(1, False), (2, False), (3, False), (3, True), (5, False)])
+def test_multi_gbm_parity(stocha, oracle, na, anti):
+    rng = np.random.default_rng(na)
+    s0 = list(rng.uniform(50, 200, na))
+    mu = list(rng.uniform(0.0, 0.1, na))
+    sig = list(rng.uniform(0.1, 0.4, na))
+    a = rng.normal(size=(na, na))
+    cov = a @ a.T + na * np.eye(na)
+    d = np.sqrt(np.diag(cov))
+    corr = cov / np.outer(d, d)
+    got = stocha.multi_gbm(s0, mu, sig, corr, 1.0, 60, 501, seed=9, antithetic=anti)
+    want = oracle.multi_gbm(s0, mu, sig, corr, 1.0, 60, 501, seed=9, antithetic=anti)
+    assert got.shape == (501, 61, na)
+    assert _rel(got, want) <= PATH_RTOL
+
+
+@pytest.mark.parametrize("scheme", ["euler", "qe"])
+def test_heston_parity(stocha, oracle, scheme):
+    kw = dict(s0=100.0, v0=0.04, mu=0.05, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7, t=1.0, steps=252, n_paths=1500,
+              seed=42)
+    got = stocha.heston(**kw, scheme=scheme)
+    want = oracle.heston(*[kw[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t", "steps",
+                                           "n_paths")], seed=42, scheme=scheme)
+    assert _rel(got, want) <= PATH_RTOL
+    # Feller-violating parameters (reference tests: kappa=1 with QE)
+    got = stocha.heston(100.0, 0.04, 0.05, 1.0, 0.04, 0.3, -0.7, 1.0, 252, 700, seed=77, scheme=scheme)
+    want = oracle.heston(100.0, 0.04, 0.05, 1.0, 0.04, 0.3, -0.7, 1.0, 252, 700, seed=77, scheme=scheme)
+    assert _rel(got, want) <= PATH_RTOL and (got > 0).all()
+
+
+def test_merton_parity(stocha, oracle):
+    for lam, mu_j, sj in [(1.0, -0.05, 0.1), (0.0, 0.0, 0.0), (5.0, -0.2, 0.15), (200.0, 0.01, 0.3)]:
+        got = stocha.merton_jump_diffusion(100.0, 0.05, 0.2, lam, mu_j, sj, 1.0, 252, 1200, seed=42)
+        want = oracle.merton(100.0, 0.05, 0.2, lam, mu_j, sj, 1.0, 252, 1200, seed=42)
+        assert _rel(got, want) <= PATH_RTOL, lam
+
+
+@pytest.mark.slow
+def test_config2_prefix_rows_full_size(stocha, oracle):
+    """1e6-path runs: rows depend on their own index only, so the first rows
+    of the full run equal an oracle run of those rows."""
+    n, k = 1_000_000, 20_000
+    corr = np.array([[1, .6, .3], [.6, 1, .5], [.3, .5, 1]], float)
+    got = stocha.multi_gbm([100, 50, 200], [0.05, 0.08, 0.03], [0.2, 0.3, 0.15], corr, 1.0, 252, n, seed=42)
+    want = oracle.multi_gbm([100, 50, 200], [0.05, 0.08, 0.03], [0.2, 0.3, 0.15], corr, 1.0, 252, k, seed=42)
+    assert _rel(got[:k], want) <= PATH_RTOL
+    assert np.isfinite(got).all() and (got > 0).all()
+    del got
+    got = stocha.heston(100, 0.04, 0.05, 2.0, 0.04, 0.3, -0.7, 1.0, 252, n, seed=42)
+    want = oracle.heston(100, 0.04, 0.05, 2.0, 0.04, 0.3, -0.7, 1.0, 252, k, seed=42)
+    assert _rel(got[:k], want) <= PATH_RTOL
+    del got
+    got = stocha.merton_jump_diffusion(100, 0.05, 0.2, 1.0, -0.05, 0.1, 1.0, 252, n, seed=42)
+    want = oracle.merton(100, 0.05, 0.2, 1.0, -0.05, 0.1, 1.0, 252, k, seed=42)
+    assert _rel(got[:k], want) <= PATH_RTOL
