@@ -39,7 +39,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_PATHS = 1_000_000
+N_PATHS = 1_000_000  # --paths overrides (small cases for profiling only)
 STEPS = 252
 SEED = 42
 STRIKE = 100.0
@@ -251,12 +251,12 @@ def run_ours(args, rank, world):
     # ---- e2e FP32 fused through the public API
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(0 if args.skip_e2e else args.steps):
         for name, p in WORKLOAD:
             stocha.price_european(name, p, STRIKE, steps=STEPS, n_paths=N_PATHS, seed=seed, precision="fp32",
                                   rate=0.05)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
-    e2e = world * path_steps / e2e_s
+    e2e = world * path_steps / e2e_s if not args.skip_e2e else None
 
     # ---- FP64 plain: materialised paths, device resident and end to end
     fp64 = {}
@@ -337,13 +337,16 @@ def run_ours(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-e2e64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--paths", type=int, default=N_PATHS, help="paths per model (profiling cases)")
     args = ap.parse_args()
+    globals()["N_PATHS"] = args.paths
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
