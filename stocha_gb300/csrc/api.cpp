@@ -378,6 +378,40 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
   }
 }
 
+void fill_f32_constants(PathLaunch* L) {
+  F32K& f = L->f32;
+  const double steps = (double)L->steps;
+  f.strike = (float)L->strike;
+  f.g_s0 = (float)L->gbm.s0;
+  f.g_kdrift = (float)(steps * L->gbm.drift);
+  f.g_diff = (float)L->gbm.diffusion;
+  f.g_drift = (float)L->gbm.drift;
+  f.m_s0 = (float)L->merton.s0;
+  f.m_kdrift = (float)(steps * L->merton.drift);
+  f.m_diff = (float)L->merton.diffusion;
+  f.m_drift = (float)L->merton.drift;
+  f.m_mu_j = (float)L->merton.mu_j;
+  f.m_sigma_j = (float)L->merton.sigma_j;
+  const HestonK& h = L->heston;
+  f.h_s0 = (float)h.s0;
+  f.h_v0 = (float)h.v0;
+  f.h_rho = (float)h.rho;
+  f.h_rho_comp = (float)h.rho_comp;
+  f.h_kdt = (float)(h.kappa * h.dt);
+  f.h_theta = (float)h.theta;
+  f.h_xsdt = (float)(h.xi * h.sqrt_dt);
+  f.h_nhdt = (float)(-0.5 * h.dt);
+  f.h_mudt = (float)(h.mu * h.dt);
+  f.h_sdt = (float)h.sqrt_dt;
+  for (int i = 0; i < kMaxAssets; ++i) {
+    f.a_s0[i] = (float)L->multi.s0[i];
+    f.a_kdrift[i] = (float)(steps * L->multi.drift[i]);
+    f.a_diff[i] = (float)L->multi.diffusion[i];
+    f.a_drift[i] = (float)L->multi.drift[i];
+    for (int j = 0; j < kMaxAssets; ++j) f.a_L[i * kMaxAssets + j] = (float)L->multi.L[i * kMaxAssets + j];
+  }
+}
+
 // Materialises the paths of `m` into device memory (async, ctx stream).
 static int paths_to_device(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precision, void* out_dev) {
   PathLaunch L;
@@ -388,6 +422,7 @@ static int paths_to_device(stocha_ctx* c, const stocha_model* m, uint64_t seed, 
   make_stream_spec((u128)seed, block, &L.ss);
   L.tabs = c->d_tabs;
   L.err = c->d_err;
+  fill_f32_constants(&L);
   if (precision == STOCHA_FP32)
     L.out_f32 = (float*)out_dev;
   else
@@ -432,6 +467,7 @@ static int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int
   L.err = c->d_err;
   L.strike = strike;
   L.payoff = payoff;
+  fill_f32_constants(&L);
   const int na = m->kind == STOCHA_MODEL_MULTI_GBM ? m->n_assets : 1;
   // partial records: at most (SMs * 64) blocks of 2*na doubles
   int sms = 152;
@@ -459,7 +495,7 @@ void stocha_ctx_destroy(stocha_ctx* c) {
   if (c == g_default) return;  // the default context lives until exit
   DeviceGuard g(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  for (DevBuf* b : {&c->out, &c->partials, &c->small, &c->aux})
+  for (DevBuf* b : {&c->out, &c->partials, &c->small, &c->aux, &c->starts})
     if (b->ptr) cudaFree(b->ptr);
   if (c->d_tabs) cudaFree(c->d_tabs);
   if (c->d_err) cudaFree(c->d_err);

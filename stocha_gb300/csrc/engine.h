@@ -35,6 +35,18 @@ struct MultiK {  // multi_gbm.rs:22-40
   double L[kMaxAssets * kMaxAssets];  // lower Cholesky factor, row-major
 };
 
+// FP32 constants of the FP32 kernels, rounded once on the host: a double
+// operation or a double->float conversion inside a kernel runs on the FP64
+// pipe (1/64 of the FP32 rate on GB300), which these kernels avoid entirely.
+struct F32K {
+  float strike;
+  float g_s0, g_kdrift, g_diff, g_drift;  // GBM: kdrift = steps * drift
+  float m_s0, m_kdrift, m_diff, m_drift, m_mu_j, m_sigma_j;  // Merton
+  float h_s0, h_v0, h_rho, h_rho_comp, h_kdt, h_theta, h_xsdt, h_nhdt, h_mudt, h_sdt;  // Heston Euler
+  float a_s0[kMaxAssets], a_kdrift[kMaxAssets], a_diff[kMaxAssets], a_drift[kMaxAssets];
+  float a_L[kMaxAssets * kMaxAssets];
+};
+
 // One launch of a path kernel over output rows [row_begin, row_begin+rows).
 struct PathLaunch {
   StreamSpec ss;
@@ -54,7 +66,11 @@ struct PathLaunch {
   HestonK heston;
   MertonK merton;
   MultiK multi;
+  F32K f32;
 };
+
+// Rounds the FP32 constants of L (after the model constants are set).
+void fill_f32_constants(PathLaunch* L);
 
 // Launch helpers (paths_f64.cu / paths_f32.cu).  Return the number of blocks
 // launched (= number of partial records in fused mode), or -1 on error.

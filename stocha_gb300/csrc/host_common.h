@@ -29,7 +29,7 @@ struct stocha_ctx {
   unsigned* d_err = nullptr;
   unsigned* h_err = nullptr;  // pinned
   double* h_small = nullptr;  // pinned, 4096 doubles for small results
-  stocha::DevBuf out, partials, small, aux;
+  stocha::DevBuf out, partials, small, aux, starts;
   std::recursive_mutex mu;
 };
 

@@ -57,15 +57,17 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
     Kahan w;
+    float kf = 0.0f;  // step count as float (no per-step integer conversion)
     if (kStore) store32(a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       float z = normal_f32(s, c, zs, err);
       w.add(neg ? -z : z);
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf((float)k * drift + diffusion * w.value()));
+      kf += 1.0f;
+      if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf(fmaf(kf, drift, diffusion * w.value())));
     }
     if (!kStore) {
-      float sT = s0 * __expf((float)a.steps * drift + diffusion * w.value());
+      float sT = s0 * __expf(fmaf(diffusion, w.value(), a.f32.g_kdrift));
       float p = payoff_f32(sT, strike, a.payoff);
       acc.add(p);
       acc2.add(p * p);
@@ -90,8 +92,10 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
     Kahan w[CAP];
+    const F32K& f = a.f32;
+    float kf = 0.0f;
     if (kStore)
-      for (int i = 0; i < na; ++i) store32(a, lrow, 0, na, i, (float)a.multi.s0[i]);
+      for (int i = 0; i < na; ++i) store32(a, lrow, 0, na, i, f.a_s0[i]);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
 #pragma unroll
@@ -99,14 +103,15 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
         float z = normal_f32(s, c, zs, err);
         w[i].add(neg ? -z : z);
       }
+      kf += 1.0f;
       if (kStore) {
 #pragma unroll
         for (int i = 0; i < na; ++i) {
           float eps = 0.0f;
 #pragma unroll
-          for (int m = 0; m <= i; ++m) eps = fmaf((float)a.multi.L[i * kMaxAssets + m], w[m].value(), eps);
-          float lg = (float)k * (float)a.multi.drift[i] + (float)a.multi.diffusion[i] * eps;
-          store32(a, lrow, k, na, i, (float)a.multi.s0[i] * __expf(lg));
+          for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
+          float lg = fmaf(kf, f.a_drift[i], f.a_diff[i] * eps);
+          store32(a, lrow, k, na, i, f.a_s0[i] * __expf(lg));
         }
       }
     }
@@ -115,9 +120,9 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
       for (int i = 0; i < na; ++i) {
         float eps = 0.0f;
 #pragma unroll
-        for (int m = 0; m <= i; ++m) eps = fmaf((float)a.multi.L[i * kMaxAssets + m], w[m].value(), eps);
-        float lg = (float)a.steps * (float)a.multi.drift[i] + (float)a.multi.diffusion[i] * eps;
-        float p = payoff_f32((float)a.multi.s0[i] * __expf(lg), (float)a.strike, a.payoff);
+        for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
+        float lg = fmaf(f.a_diff[i], eps, f.a_kdrift[i]);
+        float p = payoff_f32(f.a_s0[i] * __expf(lg), f.strike, a.payoff);
         acc[i].add(p);
         acc2[i].add(p * p);
       }
@@ -160,7 +165,7 @@ __global__ void __launch_bounds__(256) k_heston_euler_f32(const __grid_constant_
       if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf(lg.value()));
     }
     if (!kStore) {
-      float p = payoff_f32(s0 * __expf(lg.value()), (float)a.strike, a.payoff);
+      float p = payoff_f32(s0 * __expf(lg.value()), a.f32.strike, a.payoff);
       acc.add(p);
       acc2.add(p * p);
     }
@@ -184,18 +189,19 @@ __global__ void __launch_bounds__(256) k_merton_f32(const __grid_constant__ Path
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     Kahan w;
-    float jumps = 0.0f;
+    float jumps = 0.0f, kf = 0.0f;
     if (kStore) store32(a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       w.add(normal_f32(s, c, zs, err));
       uint64_t u = s.next();
       if ((u >> 11) < M.jump_thr) jumps += fmaf(sigma_j, normal_f32(s, c, zs, err), mu_j);
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf((float)k * drift + diffusion * w.value() + jumps));
+      kf += 1.0f;
+      if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf(fmaf(kf, drift, diffusion * w.value()) + jumps));
     }
     if (!kStore) {
-      float sT = s0 * __expf((float)a.steps * drift + diffusion * w.value() + jumps);
-      float p = payoff_f32(sT, (float)a.strike, a.payoff);
+      float sT = s0 * __expf(fmaf(diffusion, w.value(), a.f32.m_kdrift) + jumps);
+      float p = payoff_f32(sT, a.f32.strike, a.payoff);
       acc.add(p);
       acc2.add(p * p);
     }
@@ -222,12 +228,24 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int b = 256;
+  const bool store = L.out_f32 != nullptr;
+  // Persistent grid: exactly the blocks that are resident at once, so the
+  // grid-stride loop gives every thread the same number of paths (+-1) in a
+  // single wave instead of a partial second wave of blocks.
+  const void* fn = nullptr;
+  switch (L.model) {
+    case kGbm: fn = store ? (const void*)k_gbm_f32<true> : (const void*)k_gbm_f32<false>; break;
+    case kHeston: fn = store ? (const void*)k_heston_euler_f32<true> : (const void*)k_heston_euler_f32<false>; break;
+    case kMerton: fn = store ? (const void*)k_merton_f32<true> : (const void*)k_merton_f32<false>; break;
+    default: fn = store ? (const void*)k_multi_gbm_f32<3, true> : (const void*)k_multi_gbm_f32<3, false>; break;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, b, 0) != cudaSuccess || per_sm < 1) per_sm = 2;
   uint64_t g = (L.rows + b - 1) / b;
-  const uint64_t cap = (uint64_t)sms * 8;  // grid-stride: 8 resident blocks of 256 per SM
+  const uint64_t cap = (uint64_t)sms * per_sm;
   if (g > cap) g = cap;
   if (g < 1) g = 1;
   dim3 G((unsigned)g), B(b);
-  const bool store = L.out_f32 != nullptr;
   switch (L.model) {
     case kGbm:
       if (store) k_gbm_f32<true><<<G, B, 0, st>>>(L); else k_gbm_f32<false><<<G, B, 0, st>>>(L);

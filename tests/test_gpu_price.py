@@ -57,6 +57,29 @@ def test_fp32_fused_within_1e4_of_fp64(stocha, model):
     assert abs(p32 - p64) <= FP32_PRICE_RTOL * abs(p64), (p32, p64)
 
 
+@pytest.mark.parametrize("n", [1, 2, 1001, 300_001])
+def test_antithetic_fused(stocha, oracle, n):
+    p = MODELS["gbm"]
+    kw = dict(strike=100.0, payoff="call", steps=52, n_paths=n, seed=11, antithetic=True)
+    p64, _ = stocha.price_european("gbm", p, precision="fp64", **kw)
+    p32, _ = stocha.price_european("gbm", p, precision="fp32", **kw)
+    paths = oracle.gbm(p["s0"], p["mu"], p["sigma"], p["t"], 52, n, seed=11, antithetic=True)
+    want = math.exp(-0.05) * np.maximum(paths[:, -1] - 100.0, 0).sum() / n
+    assert abs(p64 - want) <= FP64_PRICE_RTOL * max(abs(want), 1e-12)
+    assert abs(p32 - p64) <= FP32_PRICE_RTOL * max(abs(p64), 1e-3)
+
+
+def test_fused_small_and_uneven_counts(stocha):
+    # fewer paths than lanes, and counts that do not divide the grid
+    for n in (1, 7, 255, 257, 4099):
+        for model in ("gbm", "heston", "merton"):
+            p64, _ = stocha.price_european(model, MODELS[model], 100.0, steps=12, n_paths=n, seed=3,
+                                           precision="fp64")
+            p32, _ = stocha.price_european(model, MODELS[model], 100.0, steps=12, n_paths=n, seed=3,
+                                           precision="fp32")
+            assert abs(p32 - p64) <= FP32_PRICE_RTOL * max(abs(p64), 1e-2), (model, n, p32, p64)
+
+
 def test_multi_asset_fused(stocha, oracle):
     corr = np.array([[1, .6, .3], [.6, 1, .5], [.3, .5, 1]], float)
     m = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.15], corr=corr, t=1.0)
