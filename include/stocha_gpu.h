@@ -129,6 +129,20 @@ int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t 
 int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
                         double strike, double rate, double* out_dev);
 
+/* ----------------------------------------------------------------- LSMC */
+/* replaces #[pyfunction] lsmc_american_option, src/lib.rs:854-918 ->
+ * finance/lsmc.rs:25 lsmc_american_option.  FP64 paths (the reference's),
+ * FP64 regression by normal equations.  Writes the price and its standard
+ * error. */
+int stocha_lsmc_american_option(stocha_ctx* ctx, double s0, double k, double r, double sigma, double t,
+                                uint64_t steps, uint64_t n_paths, int32_t is_put, uint64_t poly_degree,
+                                uint64_t seed, double* price, double* std_err);
+/* Same with the path precision chosen (STOCHA_FP32: FP32 paths, FP64
+ * regression); no counterpart in the reference. */
+int stocha_lsmc(stocha_ctx* ctx, double s0, double k, double r, double sigma, double t, uint64_t steps,
+                uint64_t n_paths, int32_t is_put, uint64_t poly_degree, uint64_t seed, int32_t precision,
+                double* price, double* std_err);
+
 /* ------------------------------------------------------------------ RNG
  * replaces #[pyclass] RNG, src/lib.rs:74-184 (-> prng/pcg64.rs, dist/normal.rs).
  * The state lives on the host (it is 48 bytes); draws are generated on the

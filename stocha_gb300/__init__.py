@@ -31,6 +31,7 @@ __all__ = [
     "heston",
     "merton_jump_diffusion",
     "multi_gbm",
+    "lsmc_american_option",
     "price_european",
     "model_struct",
     "__version__",
@@ -102,6 +103,16 @@ def multi_gbm(s0: list, mu: list, sigma: list, corr: np.ndarray, t: float, steps
     (python/stocha/__init__.py:574-627)."""
     return _stocha.multi_gbm(s0=list(s0), mu=list(mu), sigma=list(sigma), corr=np.asarray(corr, dtype=np.float64),
                              t=t, steps=steps, n_paths=n_paths, seed=seed, antithetic=antithetic)
+
+
+def lsmc_american_option(s0: float, k: float, r: float, sigma: float, t: float, steps: int, n_paths: int,
+                         is_put: bool = True, poly_degree: int = 3, seed: int = 42,
+                         precision: str = "fp64") -> tuple[float, float]:
+    """American option by Longstaff-Schwartz, ``(price, std_err)``
+    (python/stocha/__init__.py:630-671).  ``precision="fp32"`` is a GB300
+    addition: FP32 paths with the FP64 regression."""
+    return _stocha.lsmc_american_option(s0=s0, k=k, r=r, sigma=sigma, t=t, steps=steps, n_paths=n_paths,
+                                        is_put=is_put, poly_degree=poly_degree, seed=seed, precision=precision)
 
 
 # ------------------------------------------------------- GB300 additions ---

@@ -77,6 +77,9 @@ SIGNATURES = [
     ("stocha_rng_save_state", c_i32, [ctypes.POINTER(StochaRng), ctypes.c_char_p, c_size, ctypes.POINTER(c_size)]),
     ("stocha_rng_from_state", c_i32, [c_char_p, ctypes.POINTER(StochaRng)]),
     ("stocha_rng_raw_u64", c_i32, [c_void_p, ctypes.POINTER(StochaRng), c_u64, P_u64]),
+    ("stocha_lsmc_american_option", c_i32, [c_void_p] + [c_dbl] * 5 + [c_u64, c_u64, c_i32, c_u64, c_u64, P_dbl,
+                                                                   P_dbl]),
+    ("stocha_lsmc", c_i32, [c_void_p] + [c_dbl] * 5 + [c_u64, c_u64, c_i32, c_u64, c_u64, c_i32, P_dbl, P_dbl]),
     ("stocha_debug_zig_thresholds", c_i32, [P_u64]),
     ("stocha_measure_peak", c_i32, [c_void_p, c_i32, P_dbl]),
 ]

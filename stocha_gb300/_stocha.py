@@ -172,6 +172,26 @@ def multi_gbm(s0, mu, sigma, corr, t, steps, n_paths, seed=42, antithetic=False)
     return out
 
 
+def lsmc_american_option(s0, k, r, sigma, t, steps, n_paths, is_put=True, poly_degree=3, seed=42,
+                         precision="fp64"):
+    """lib.rs:854-918: (price, std_err) of an American option by LSMC.
+    ``precision="fp32"`` (no counterpart in the reference) runs the paths in
+    FP32; the regression stays FP64."""
+    vals = [_f64(v, nm) for v, nm in zip((s0, k, r, sigma, t), ("s0", "k", "r", "sigma", "t"))]
+    steps, n_paths = _usize(steps, "steps"), _usize(n_paths, "n_paths")
+    is_put, deg, seed = _bool(is_put, "is_put"), _usize(poly_degree, "poly_degree"), _usize(seed, "seed")
+    if precision not in ("fp64", "fp32"):
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    price, se = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    if precision == "fp64":
+        check(load().stocha_lsmc_american_option(None, *vals, steps, n_paths, int(is_put), deg, seed,
+                                                 ctypes.byref(price), ctypes.byref(se)))
+    else:
+        check(load().stocha_lsmc(None, *vals, steps, n_paths, int(is_put), deg, seed,
+                                 _lib.FP32 if precision == "fp32" else -1, ctypes.byref(price), ctypes.byref(se)))
+    return float(price.value), float(se.value)
+
+
 def _alloc(n_paths, cols, plausible, n_assets=None):
     """Output array; tiny placeholder when validation is about to fail."""
     if not plausible or n_paths == 0 or cols <= 1:

@@ -28,7 +28,7 @@ CUDA_UNITS = {
     "paths_f64.cu": ["--fmad=false"],
     "paths_f32.cu": [],
     "rng.cu": ["--fmad=false"],
-    "lsmc.cu": ["--fmad=false"],
+    "lsmc.cu": [],
     "greeks.cu": [],
     "batch.cu": [],
     "peaks.cu": [],

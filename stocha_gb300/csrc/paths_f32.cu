@@ -64,10 +64,10 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
       float z = normal_f32(s, c, zs, err);
       w.add(neg ? -z : z);
       kf += 1.0f;
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf(fmaf(kf, drift, diffusion * w.value())));
+      if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value())));
     }
     if (!kStore) {
-      float sT = s0 * __expf(fmaf(diffusion, w.value(), a.f32.g_kdrift));
+      float sT = s0 * expf(fmaf(diffusion, w.value(), a.f32.g_kdrift));
       float p = payoff_f32(sT, strike, a.payoff);
       acc.add(p);
       acc2.add(p * p);
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
 #pragma unroll
           for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
           float lg = fmaf(kf, f.a_drift[i], f.a_diff[i] * eps);
-          store32(a, lrow, k, na, i, f.a_s0[i] * __expf(lg));
+          store32(a, lrow, k, na, i, f.a_s0[i] * expf(lg));
         }
       }
     }
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
 #pragma unroll
         for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
         float lg = fmaf(f.a_diff[i], eps, f.a_kdrift[i]);
-        float p = payoff_f32(f.a_s0[i] * __expf(lg), f.strike, a.payoff);
+        float p = payoff_f32(f.a_s0[i] * expf(lg), f.strike, a.payoff);
         acc[i].add(p);
         acc2[i].add(p * p);
       }
@@ -162,10 +162,10 @@ __global__ void __launch_bounds__(256) k_heston_euler_f32(const __grid_constant_
       float sqrt_v = sqrtf(v_plus);
       v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
       lg.add(fmaf(-half_dt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf(lg.value()));
+      if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(lg.value()));
     }
     if (!kStore) {
-      float p = payoff_f32(s0 * __expf(lg.value()), a.f32.strike, a.payoff);
+      float p = payoff_f32(s0 * expf(lg.value()), a.f32.strike, a.payoff);
       acc.add(p);
       acc2.add(p * p);
     }
@@ -197,10 +197,10 @@ __global__ void __launch_bounds__(256) k_merton_f32(const __grid_constant__ Path
       uint64_t u = s.next();
       if ((u >> 11) < M.jump_thr) jumps += fmaf(sigma_j, normal_f32(s, c, zs, err), mu_j);
       kf += 1.0f;
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * __expf(fmaf(kf, drift, diffusion * w.value()) + jumps));
+      if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value()) + jumps));
     }
     if (!kStore) {
-      float sT = s0 * __expf(fmaf(diffusion, w.value(), a.f32.m_kdrift) + jumps);
+      float sT = s0 * expf(fmaf(diffusion, w.value(), a.f32.m_kdrift) + jumps);
       float p = payoff_f32(sT, a.f32.strike, a.payoff);
       acc.add(p);
       acc2.add(p * p);

@@ -123,3 +123,21 @@ def test_rng_seed_state_matches_oracle(stocha, oracle):
         st, inc = oracle.pcg_seed(seed)
         js = r.save_state()
         assert f'"state":{st},' in js and f'"increment":{inc}}}' in js
+
+
+def test_lsmc_validation_messages(stocha):
+    f = stocha.lsmc_american_option
+    cases = [
+        (lambda: f(-1.0, 100.0, 0.05, 0.2, 1.0, 10, 100), "s0 must be positive"),
+        (lambda: f(100.0, 0.0, 0.05, 0.2, 1.0, 10, 100), "k must be positive"),
+        (lambda: f(100.0, 100.0, 0.05, 0.0, 1.0, 10, 100), "sigma must be positive"),
+        (lambda: f(100.0, 100.0, 0.05, 0.2, 0.0, 10, 100), "t must be positive"),
+        (lambda: f(100.0, 100.0, 0.05, 0.2, 1.0, 0, 100), "steps and n_paths must be positive"),
+        (lambda: f(100.0, 100.0, 0.05, 0.2, 1.0, 10, 1), "n_paths must be at least 2"),
+        (lambda: f(100.0, 100.0, 0.05, 0.2, 1.0, 10, 100, poly_degree=0), "poly_degree must be in [1, 4]"),
+        (lambda: f(100.0, 100.0, 0.05, 0.2, 1.0, 10, 100, poly_degree=5), "poly_degree must be in [1, 4]"),
+    ]
+    for fn, msg in cases:
+        with pytest.raises(ValueError) as ei:
+            fn()
+        assert str(ei.value) == msg
