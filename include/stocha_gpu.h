@@ -143,6 +143,61 @@ int stocha_lsmc(stocha_ctx* ctx, double s0, double k, double r, double sigma, do
                 uint64_t n_paths, int32_t is_put, uint64_t poly_degree, uint64_t seed, int32_t precision,
                 double* price, double* std_err);
 
+/* --------------------------------------------------------------- Greeks */
+/* Model parameters of greeks_fd (the reference takes a dict, lib.rs:958-1040).
+ * `present` has bit i set when field i (in declaration order: s0, r, sigma,
+ * t, v0, kappa, theta, xi, rho, lambda_, mu_j, sigma_j) was given; the first
+ * missing required key is reported as the reference does.  scheme: Heston
+ * 0 euler, 1 qe, -1 for an unknown name. */
+typedef struct stocha_greeks_params {
+  double s0, r, sigma, t, v0, kappa, theta, xi, rho, lambda_, mu_j, sigma_j;
+  uint32_t present;
+  int32_t scheme;
+} stocha_greeks_params;
+
+/* Custom payoff: receives the n terminal prices of one scenario and returns
+ * the sum of its payoff values (in order) and their count; non-zero return
+ * aborts with STOCHA_ERR_CALLBACK. */
+typedef int32_t (*stocha_payoff_fn)(void* user, const double* terminals, uint64_t n, double* payoff_sum,
+                                    uint64_t* payoff_len);
+
+/* replaces #[pyfunction] greeks_fd, src/lib.rs:1064-1156 -> finance/greeks.rs:322
+ * greeks_fd_core.  model "gbm" | "heston" | "merton"; payoff "call" | "put",
+ * or NULL with a callback.  greeks: names ("delta", "gamma", "vega",
+ * "theta", "rho"); out[i] receives greeks[i].  precision STOCHA_FP64 runs the
+ * reference's scenario-by-scenario revaluation; STOCHA_FP32 (built-in payoffs,
+ * Heston euler) runs all scenarios of every path in one pass with common
+ * random numbers. */
+int stocha_greeks_fd(stocha_ctx* ctx, const char* model, const stocha_greeks_params* params, const char* payoff,
+                     stocha_payoff_fn payoff_cb, void* user, double strike, uint64_t n_paths, uint64_t n_steps,
+                     const char* const* greeks, uint64_t n_greeks, uint64_t seed, double bump_size,
+                     int32_t precision, double* out);
+
+/* replaces #[pyfunction] greeks_pathwise, src/lib.rs:1177-1242 ->
+ * finance/greeks.rs:360 greeks_pathwise_core (GBM; "delta", "vega"). */
+int stocha_greeks_pathwise(stocha_ctx* ctx, double s0, double r, double sigma, double t, double strike,
+                           int32_t is_call, uint64_t n_paths, uint64_t n_steps, const char* const* greeks,
+                           uint64_t n_greeks, uint64_t seed, double* out);
+
+/* One instance of a batched Greeks run (no counterpart call in the
+ * reference: each instance is one greeks_fd(model, params, payoff, strike,
+ * n_paths, steps, all five greeks, seed, bump_size) call). */
+typedef struct stocha_greeks_instance {
+  int32_t model;  /* STOCHA_MODEL_GBM / _HESTON / _MERTON */
+  int32_t payoff; /* STOCHA_PAYOFF_CALL / _PUT */
+  int32_t scheme; /* Heston: 0 euler, 1 qe */
+  int32_t pad;
+  double s0, r, sigma, t, v0, kappa, theta, xi, rho, lambda_, mu_j, sigma_j, strike, bump_size;
+  uint64_t n_paths, steps, seed;
+} stocha_greeks_instance;
+
+/* Prices and Greeks of n instances in one persistent launch (FP32 paths,
+ * FP64 reductions) or, with STOCHA_FP64, instance by instance with the
+ * reference's scenario revaluation.  out[7*i .. 7*i+6] = price, its standard
+ * error, delta, gamma, vega, theta, rho. */
+int stocha_greeks_batch(stocha_ctx* ctx, const stocha_greeks_instance* inst, uint64_t n, int32_t precision,
+                        double* out);
+
 /* ------------------------------------------------------------------ RNG
  * replaces #[pyclass] RNG, src/lib.rs:74-184 (-> prng/pcg64.rs, dist/normal.rs).
  * The state lives on the host (it is 48 bytes); draws are generated on the

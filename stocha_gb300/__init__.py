@@ -32,6 +32,9 @@ __all__ = [
     "merton_jump_diffusion",
     "multi_gbm",
     "lsmc_american_option",
+    "greeks_fd",
+    "greeks_pathwise",
+    "greeks_batch",
     "price_european",
     "model_struct",
     "__version__",
@@ -115,7 +118,54 @@ def lsmc_american_option(s0: float, k: float, r: float, sigma: float, t: float, 
                                         is_put=is_put, poly_degree=poly_degree, seed=seed, precision=precision)
 
 
+def greeks_fd(model: str, params: dict, payoff, strike: float, n_paths: int, n_steps: int, greeks: list,
+              seed: int = 42, bump_size: float = 0.01, precision: str = "fp64") -> dict:
+    """Bump-and-revalue Greeks with common random numbers
+    (python/stocha/__init__.py:674-722).  ``precision="fp32"`` is a GB300
+    addition: every scenario of a path in one FP32 pass."""
+    return _stocha.greeks_fd(model=model, params=params, payoff=payoff, strike=strike, n_paths=n_paths,
+                             n_steps=n_steps, greeks=greeks, seed=seed, bump_size=bump_size, precision=precision)
+
+
+def greeks_pathwise(s0: float, r: float, sigma: float, t: float, strike: float, is_call: bool, n_paths: int,
+                    n_steps: int, greeks: list, seed: int = 42) -> dict:
+    """Pathwise (IPA) delta and vega for GBM (python/stocha/__init__.py:725-769)."""
+    return _stocha.greeks_pathwise(s0=s0, r=r, sigma=sigma, t=t, strike=strike, is_call=is_call, n_paths=n_paths,
+                                   n_steps=n_steps, greeks=greeks, seed=seed)
+
+
 # ------------------------------------------------------- GB300 additions ---
+_BATCH_FIELDS = ("s0", "r", "sigma", "t", "v0", "kappa", "theta", "xi", "rho", "lambda_", "mu_j", "sigma_j")
+
+
+def greeks_batch(instances: list, precision: str = "fp32"):
+    """Price and all five Greeks of many instances in one persistent launch.
+
+    Each instance is a dict: ``model`` ("gbm"/"heston"/"merton"), the
+    model's parameters as for greeks_fd (``r`` is the drift), ``strike``,
+    ``payoff`` ("call"/"put", default call), ``n_paths``, ``steps``,
+    optional ``seed`` (42), ``bump_size`` (0.01), ``scheme`` (Heston).
+    ``precision="fp32"``: FP32 paths with common random numbers across
+    scenarios and FP64 reductions; ``"fp64"``: the reference's scenario
+    revaluation per instance.  Returns an array (n, 7): price, std_err,
+    delta, gamma, vega, theta, rho."""
+    n = len(instances)
+    arr = (_lib.StochaGreeksInstance * max(n, 1))()
+    for i, d in enumerate(instances):
+        x = arr[i]
+        x.model = _KINDS[d["model"]]
+        x.payoff = _lib.PAYOFF_CALL if d.get("payoff", "call") == "call" else _lib.PAYOFF_PUT
+        x.scheme = 1 if d.get("scheme", "euler") == "qe" else 0
+        for k in _BATCH_FIELDS:
+            setattr(x, k, float(d.get(k, 0.0)))
+        x.strike = float(d["strike"])
+        x.bump_size = float(d.get("bump_size", 0.01))
+        x.n_paths, x.steps, x.seed = int(d["n_paths"]), int(d["steps"]), int(d.get("seed", 42))
+    out = np.zeros((max(n, 1), 7), np.float64)
+    if precision not in _PRECISION:
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    _lib.check(_lib.load().stocha_greeks_batch(None, arr, n, _PRECISION[precision], _lib.dptr(out)))
+    return out[:n]
 _KINDS = {"gbm": _lib.MODEL_GBM, "heston": _lib.MODEL_HESTON, "merton": _lib.MODEL_MERTON,
           "multi_gbm": _lib.MODEL_MULTI_GBM}
 _PRECISION = {"fp64": _lib.FP64, "fp32": _lib.FP32}

@@ -47,6 +47,22 @@ class StochaModel(ctypes.Structure):
     ]
 
 
+class StochaGreeksParams(ctypes.Structure):
+    _fields_ = [(k, c_dbl) for k in ("s0", "r", "sigma", "t", "v0", "kappa", "theta", "xi", "rho", "lambda_", "mu_j",
+                                     "sigma_j")] + [("present", ctypes.c_uint32), ("scheme", c_i32)]
+
+
+class StochaGreeksInstance(ctypes.Structure):
+    _fields_ = [("model", c_i32), ("payoff", c_i32), ("scheme", c_i32), ("pad", c_i32)] + \
+        [(k, c_dbl) for k in ("s0", "r", "sigma", "t", "v0", "kappa", "theta", "xi", "rho", "lambda_", "mu_j",
+                              "sigma_j", "strike", "bump_size")] + \
+        [("n_paths", c_u64), ("steps", c_u64), ("seed", c_u64)]
+
+
+PAYOFF_FN = ctypes.CFUNCTYPE(c_i32, c_void_p, P_dbl, c_u64, P_dbl, ctypes.POINTER(c_u64))
+P_charp = ctypes.POINTER(ctypes.c_char_p)
+
+
 class StochaRng(ctypes.Structure):
     _fields_ = [("state_lo", c_u64), ("state_hi", c_u64), ("inc_lo", c_u64), ("inc_hi", c_u64),
                 ("seed_lo", c_u64), ("seed_hi", c_u64)]
@@ -80,6 +96,10 @@ SIGNATURES = [
     ("stocha_lsmc_american_option", c_i32, [c_void_p] + [c_dbl] * 5 + [c_u64, c_u64, c_i32, c_u64, c_u64, P_dbl,
                                                                    P_dbl]),
     ("stocha_lsmc", c_i32, [c_void_p] + [c_dbl] * 5 + [c_u64, c_u64, c_i32, c_u64, c_u64, c_i32, P_dbl, P_dbl]),
+    ("stocha_greeks_fd", c_i32, [c_void_p, c_char_p, ctypes.POINTER(StochaGreeksParams), c_char_p, PAYOFF_FN, c_void_p,
+                                 c_dbl, c_u64, c_u64, P_charp, c_u64, c_u64, c_dbl, c_i32, P_dbl]),
+    ("stocha_greeks_pathwise", c_i32, [c_void_p] + [c_dbl] * 5 + [c_i32, c_u64, c_u64, P_charp, c_u64, c_u64, P_dbl]),
+    ("stocha_greeks_batch", c_i32, [c_void_p, ctypes.POINTER(StochaGreeksInstance), c_u64, c_i32, P_dbl]),
     ("stocha_debug_zig_thresholds", c_i32, [P_u64]),
     ("stocha_measure_peak", c_i32, [c_void_p, c_i32, P_dbl]),
 ]

@@ -192,6 +192,98 @@ def lsmc_american_option(s0, k, r, sigma, t, steps, n_paths, is_put=True, poly_d
     return float(price.value), float(se.value)
 
 
+_GREEK_NAMES = ("delta", "gamma", "vega", "theta", "rho")
+_PARAM_KEYS = ("s0", "r", "sigma", "t", "v0", "kappa", "theta", "xi", "rho", "lambda_", "mu_j", "sigma_j")
+_MODEL_KEYS = {  # lib.rs:964-1033, in extraction order
+    "gbm": ("s0", "r", "sigma", "t"),
+    "heston": ("s0", "v0", "r", "kappa", "theta", "xi", "rho", "t"),
+    "merton": ("s0", "r", "sigma", "lambda_", "mu_j", "sigma_j", "t"),
+}
+
+
+def _greek_list(greeks):
+    if not isinstance(greeks, list):
+        raise TypeError(f"argument 'greeks': '{type(greeks).__name__}' object cannot be converted to 'PyList'")
+    names = [_str(g, "greeks") for g in greeks]
+    for g in names:  # lib.rs:920-938
+        if g not in _GREEK_NAMES:
+            raise ValueError(f"Unknown greek: '{g}'. Supported: delta, gamma, vega, theta, rho")
+    arr = (ctypes.c_char_p * max(len(names), 1))(*[g.encode() for g in names])
+    return names, arr
+
+
+def _greek_params(model, params):
+    if not isinstance(params, dict):
+        raise TypeError(f"argument 'params': '{type(params).__name__}' object cannot be converted to 'PyDict'")
+    p = _lib.StochaGreeksParams()
+    p.present = 0
+    p.scheme = 0
+    for key in _MODEL_KEYS.get(model, ()):  # lib.rs:951-956 extract_f64
+        if key not in params:
+            raise ValueError(f"Missing required param: '{key}'")
+        setattr(p, key, _f64(params[key], key))
+        p.present |= 1 << _PARAM_KEYS.index(key)
+    if model == "heston" and "scheme" in params:
+        s = _str(params["scheme"], "scheme")
+        p.scheme = 0 if s == "euler" else 1 if s == "qe" else -1
+    return p
+
+
+def greeks_fd(model, params, payoff, strike, n_paths, n_steps, greeks, seed=42, bump_size=0.01, precision="fp64"):
+    """lib.rs:1064-1156: dict of bump-and-revalue Greeks with common random
+    numbers.  ``payoff`` is "call", "put" or a callable f(terminals) -> values
+    (called once per scenario with the terminal prices, as the reference
+    does).  ``precision="fp32"`` (no counterpart in the reference) prices all
+    scenarios of each path in one FP32 pass."""
+    model = _str(model, "model")
+    strike = _f64(strike, "strike")
+    n_paths, n_steps = _usize(n_paths, "n_paths"), _usize(n_steps, "n_steps")
+    seed, bump_size = _usize(seed, "seed"), _f64(bump_size, "bump_size")
+    if not isinstance(params, dict):
+        raise TypeError(f"argument 'params': '{type(params).__name__}' object cannot be converted to 'PyDict'")
+    names, arr = _greek_list(greeks)
+    p = _greek_params(model, params)
+    if precision not in ("fp64", "fp32"):
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    out = np.zeros(max(len(names), 1), np.float64)
+    pay_name, cb, err = None, _lib.PAYOFF_FN(), []
+    if isinstance(payoff, str):
+        pay_name = payoff.encode()
+    elif callable(payoff):
+        def _cb(user, terms, n, sum_out, len_out):
+            try:
+                t = np.ctypeslib.as_array(terms, shape=(n,)).copy() if n else np.empty(0, np.float64)
+                vals = np.asarray([float(v) for v in payoff(t)], np.float64)
+                sum_out[0] = float(np.cumsum(vals)[-1]) if vals.size else 0.0  # sequential sum
+                len_out[0] = int(vals.size)
+                return 0
+            except BaseException as e:  # re-raised below
+                err.append(e)
+                return 1
+        cb = _lib.PAYOFF_FN(_cb)
+    rc = load().stocha_greeks_fd(None, model.encode(), ctypes.byref(p), pay_name, cb, None, strike, n_paths, n_steps,
+                                 arr, len(names), seed, bump_size, _lib.FP32 if precision == "fp32" else _lib.FP64,
+                                 dptr(out))
+    if err:
+        raise err[0]
+    check(rc)
+    return {g: float(v) for g, v in zip(names, out)}
+
+
+def greeks_pathwise(s0, r, sigma, t, strike, is_call, n_paths, n_steps, greeks, seed=42):
+    """lib.rs:1177-1242: pathwise (IPA) delta and vega for GBM."""
+    vals = [_f64(v, nm) for v, nm in zip((s0, r, sigma, t, strike), ("s0", "r", "sigma", "t", "strike"))]
+    is_call = _bool(is_call, "is_call")
+    n_paths, n_steps, seed = _usize(n_paths, "n_paths"), _usize(n_steps, "n_steps"), _usize(seed, "seed")
+    if not isinstance(greeks, list):
+        raise TypeError(f"argument 'greeks': '{type(greeks).__name__}' object cannot be converted to 'PyList'")
+    names = [_str(g, "greeks") for g in greeks]
+    arr = (ctypes.c_char_p * max(len(names), 1))(*[g.encode() for g in names])
+    out = np.zeros(max(len(names), 1), np.float64)
+    check(load().stocha_greeks_pathwise(None, *vals, int(is_call), n_paths, n_steps, arr, len(names), seed, dptr(out)))
+    return {g: float(v) for g, v in zip(names, out)}
+
+
 def _alloc(n_paths, cols, plausible, n_assets=None):
     """Output array; tiny placeholder when validation is about to fail."""
     if not plausible or n_paths == 0 or cols <= 1:

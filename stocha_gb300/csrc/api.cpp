@@ -241,7 +241,7 @@ std::string rust_f64(double v) {
 }
 
 // u < p with u = m*2^-53 (next_f64)  <=>  m < ceil(p*2^53)
-static uint64_t unit_threshold(double p) {
+uint64_t unit_threshold(double p) {
   if (!(p > 0.0)) return 0;  // also NaN
   double P = std::ldexp(p, 53);
   if (P >= 18446744073709551615.0) return ~0ull;
@@ -250,7 +250,7 @@ static uint64_t unit_threshold(double p) {
 
 static double powi2(double a) { return a * a; }  // Rust powi(2)
 
-int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128* block) {
+int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128* block, bool check) {
   std::memset(L, 0, sizeof *L);
   L->model = m->kind;
   L->steps = m->steps;
@@ -259,10 +259,13 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
   const double steps_f = (double)m->steps;
   switch (m->kind) {
     case STOCHA_MODEL_GBM: {  // lib.rs:219-238, gbm.rs:43-55
-      if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
-      if (m->sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
-      if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
-      if (m->steps == 0 || m->n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      if (check) {
+        if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
+        if (m->sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
+        if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+        if (m->steps == 0 || m->n_paths == 0)
+          return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      }
       const double dt = m->t / steps_f;
       L->gbm.s0 = m->s0;
       L->gbm.drift = (m->mu - m->q - 0.5 * m->sigma * m->sigma) * dt;
@@ -273,14 +276,17 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
       return STOCHA_OK;
     }
     case STOCHA_MODEL_HESTON: {  // lib.rs:342-391, heston.rs:44-150
-      if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
-      if (m->v0 < 0.0) return set_error(STOCHA_ERR_VALUE, "v0 must be non-negative");
-      if (m->kappa <= 0.0) return set_error(STOCHA_ERR_VALUE, "kappa must be positive");
-      if (m->theta <= 0.0) return set_error(STOCHA_ERR_VALUE, "theta must be positive");
-      if (m->xi <= 0.0) return set_error(STOCHA_ERR_VALUE, "xi must be positive");
-      if (m->rho < -1.0 || m->rho > 1.0) return set_error(STOCHA_ERR_VALUE, "rho must be in [-1, 1]");
-      if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
-      if (m->steps == 0 || m->n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      if (check) {
+        if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
+        if (m->v0 < 0.0) return set_error(STOCHA_ERR_VALUE, "v0 must be non-negative");
+        if (m->kappa <= 0.0) return set_error(STOCHA_ERR_VALUE, "kappa must be positive");
+        if (m->theta <= 0.0) return set_error(STOCHA_ERR_VALUE, "theta must be positive");
+        if (m->xi <= 0.0) return set_error(STOCHA_ERR_VALUE, "xi must be positive");
+        if (m->rho < -1.0 || m->rho > 1.0) return set_error(STOCHA_ERR_VALUE, "rho must be in [-1, 1]");
+        if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+        if (m->steps == 0 || m->n_paths == 0)
+          return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      }
       if (m->scheme != 0 && m->scheme != 1) return set_error(STOCHA_ERR_VALUE, "scheme must be 'euler' or 'qe'");
       HestonK& h = L->heston;
       h.s0 = m->s0;
@@ -312,12 +318,15 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
       return STOCHA_OK;
     }
     case STOCHA_MODEL_MERTON: {  // lib.rs:445-468, jump_diffusion.rs:49-64
-      if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
-      if (m->sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
-      if (m->lambda_ < 0.0) return set_error(STOCHA_ERR_VALUE, "lambda_ must be non-negative");
-      if (m->sigma_j < 0.0) return set_error(STOCHA_ERR_VALUE, "sigma_j must be non-negative");
-      if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
-      if (m->steps == 0 || m->n_paths == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      if (check) {
+        if (m->s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
+        if (m->sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
+        if (m->lambda_ < 0.0) return set_error(STOCHA_ERR_VALUE, "lambda_ must be non-negative");
+        if (m->sigma_j < 0.0) return set_error(STOCHA_ERR_VALUE, "sigma_j must be non-negative");
+        if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+        if (m->steps == 0 || m->n_paths == 0)
+          return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      }
       const double dt = m->t / steps_f;
       const double sqrt_dt = std::sqrt(dt);
       const double m_bar = std::exp(m->mu_j + 0.5 * m->sigma_j * m->sigma_j) - 1.0;
@@ -453,21 +462,29 @@ static int paths_to_host(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, 
   return finish_call(ctx);
 }
 
-static int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precision, int payoff,
-                        double strike, double* sums_dev, int* nvals) {
+int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precision, int payoff, double strike,
+                 const double* aux4, bool check, double* sums_dev, int* nvals) {
   PathLaunch L;
   uint64_t row_len = 0;
   u128 block = 0;
-  int rc = prepare_model(m, &L, &row_len, &block);
+  int rc = prepare_model(m, &L, &row_len, &block, check);
   if (rc) return rc;
-  if (payoff != STOCHA_PAYOFF_CALL && payoff != STOCHA_PAYOFF_PUT)
+  if (payoff < kCall || payoff > kPwVegaPut || (precision == STOCHA_FP32 && payoff > kPut))
     return set_error(STOCHA_ERR_VALUE, "payoff must be call or put");
   make_stream_spec((u128)seed, block, &L.ss);
   L.tabs = c->d_tabs;
   L.err = c->d_err;
   L.strike = strike;
   L.payoff = payoff;
+  if (aux4)
+    for (int i = 0; i < 4; ++i) L.aux[i] = aux4[i];
   fill_f32_constants(&L);
+  if (L.rows == 0) {  // nothing to simulate: zero sums
+    const int na0 = m->kind == STOCHA_MODEL_MULTI_GBM ? m->n_assets : 1;
+    STOCHA_CUDA(cudaMemsetAsync(sums_dev, 0, 2 * na0 * sizeof(double), c->stream));
+    *nvals = 2 * na0;
+    return STOCHA_OK;
+  }
   const int na = m->kind == STOCHA_MODEL_MULTI_GBM ? m->n_assets : 1;
   // partial records: at most (SMs * 64) blocks of 2*na doubles
   int sms = 152;
@@ -479,6 +496,23 @@ static int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int
   if (nb < 0) return cuda_error(cudaGetLastError(), "pricing kernel launch");
   launch_reduce_partials(L.partials, nb, 2 * na, sums_dev, c->stream);
   *nvals = 2 * na;
+  return STOCHA_OK;
+}
+
+int terminal_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, double* out_dev) {
+  PathLaunch L;
+  uint64_t row_len = 0;
+  u128 block = 0;
+  int rc = prepare_model(m, &L, &row_len, &block, false);
+  if (rc) return rc;
+  if (L.rows == 0) return STOCHA_OK;
+  make_stream_spec((u128)seed, block, &L.ss);
+  L.tabs = c->d_tabs;
+  L.err = c->d_err;
+  L.out_f64 = out_dev;
+  L.terminal_only = 1;
+  fill_f32_constants(&L);
+  if (launch_paths_f64(L, c->stream) < 0) return cuda_error(cudaGetLastError(), "terminal-price launch");
   return STOCHA_OK;
 }
 
@@ -651,7 +685,9 @@ int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, i
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   DeviceGuard g(ctx->device);
   int nvals = 0;
-  return price_launch(ctx, m, seed, precision, payoff, strike, out_dev, &nvals);
+  if (payoff != STOCHA_PAYOFF_CALL && payoff != STOCHA_PAYOFF_PUT)
+    return set_error(STOCHA_ERR_VALUE, "payoff must be call or put");
+  return price_launch(ctx, m, seed, precision, payoff, strike, nullptr, true, out_dev, &nvals);
 }
 
 int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
@@ -671,7 +707,9 @@ int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t 
   if ((rc = begin_call(ctx))) return rc;
   int nvals = 0;
   double* sums = (double*)ctx->small.ptr;
-  if ((rc = price_launch(ctx, m, seed, precision, payoff, strike, sums, &nvals))) return rc;
+  if (payoff != STOCHA_PAYOFF_CALL && payoff != STOCHA_PAYOFF_PUT)
+    return set_error(STOCHA_ERR_VALUE, "payoff must be call or put");
+  if ((rc = price_launch(ctx, m, seed, precision, payoff, strike, nullptr, true, sums, &nvals))) return rc;
   STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, sums, nvals * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if ((rc = finish_call(ctx))) return rc;
   const double n = (double)m->n_paths;

@@ -11,7 +11,9 @@ namespace stocha {
 constexpr int kMaxAssets = 16;
 
 enum Model : int { kGbm = 0, kHeston = 1, kMerton = 2, kMultiGbm = 3 };
-enum Payoff : int { kCall = 0, kPut = 1 };
+// In-kernel payoffs of the fused FP64 kernels.  kPw*: the pathwise (IPA)
+// estimators of greeks.rs:387-418 (aux = s0, r, sigma, t).
+enum Payoff : int { kCall = 0, kPut = 1, kPwDeltaCall = 2, kPwDeltaPut = 3, kPwVegaCall = 4, kPwVegaPut = 5 };
 
 // Model constants, computed on the host with the reference's expression order
 // so that every double the kernels start from equals the reference's.
@@ -55,11 +57,13 @@ struct PathLaunch {
   // materialised mode: row-major rows of `row_len` values (out_f64 or out_f32)
   double* out_f64;
   float* out_f32;
-  int time_major;  // 1: out[step * rows + row] (internal consumers, e.g. LSMC)
+  int time_major;     // 1: out[step * rows + row] (internal consumers, e.g. LSMC)
+  int terminal_only;  // 1: out[row] = S_T only (terminal prices, greeks.rs:165-166)
   // fused mode: per-block partial sums {sum payoff, sum payoff^2} per asset
   double* partials;
   double strike;
   int payoff;
+  double aux[4];  // payoff parameters (pathwise estimators: s0, r, sigma, t)
   uint64_t row_begin, rows, steps, base_paths;
   int model;
   GbmK gbm;

@@ -1,0 +1,236 @@
+// Batched FP32 bump-and-revalue Greeks with common random numbers.
+//
+// One persistent launch serves a queue of work items (instance, chunk of
+// paths) drawn from many instances with different models, path counts and
+// step counts.  A block takes the next item from a global counter, its
+// threads simulate the item's paths, and the block writes the item's partial
+// sums; a final pass adds each instance's items in a fixed order.
+//
+// Common random numbers (greeks.rs:322-358 prices every scenario with the
+// same seed): every path's draws are generated once and drive all scenarios.
+//   * s0 bumps: S_T is linear in s0 in all three models, so S_T(s0 +- h) =
+//     S_T * (1 +- h/s0); the payoff differences are formed per path by case
+//     analysis at the strike (no cancellation for tiny h).
+//   * drift (rho) bumps: S_T(mu +- h) = S_T * exp(+-h T) (the drift enters
+//     the log price as steps*dt*mu); same per-path differences.
+//   * sigma bumps (Heston: v0) and the T-h scenario: separate trajectories
+//     driven by the same normals (GBM and Merton in closed form from the sum
+//     of the normals; Heston as extra (v, log S) recurrences).  Merton's T-h
+//     scenario changes the jump probability and therefore the draws it
+//     consumes (jump_diffusion.rs:60,79-80): it runs as a second pass over
+//     the same stream.
+#include <cuda_runtime.h>
+
+#include "engine.h"
+#include "greeks_kernels.h"
+#include "mc_device.cuh"
+#include "reduce.cuh"
+
+namespace stocha {
+namespace {
+
+struct K32 {
+  float s, c;
+  __device__ __forceinline__ void add(float v) {
+    float y = v - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+
+__device__ __forceinline__ float pay(float s, float k, int call) { return call ? fmaxf(s - k, 0.0f) : fmaxf(k - s, 0.0f); }
+
+// First and second payoff differences for  up = S*ru, base = S, dn = S*rd
+// (ru > 1 > rd) with  up - dn = S * dud  and  up - 2 S + dn = S * d2
+// supplied exactly by the caller.
+__device__ __forceinline__ void diffs(float S, float up, float dn, float dud, float d2, float K, int call,
+                                      float* d1_out, float* g_out) {
+  float d1, g;
+  if (call) {
+    if (dn >= K) {
+      d1 = S * dud;
+      g = S * d2;
+    } else if (up <= K) {
+      d1 = 0.0f;
+      g = 0.0f;
+    } else {
+      d1 = up - K;
+      g = S <= K ? up - K : (up - K) - 2.0f * (S - K);
+    }
+  } else {
+    if (up <= K) {
+      d1 = -S * dud;
+      g = -S * d2;
+    } else if (dn >= K) {
+      d1 = 0.0f;
+      g = 0.0f;
+    } else {
+      d1 = -(K - dn);
+      g = S >= K ? K - dn : (K - dn) - 2.0f * (K - S);
+    }
+  }
+  *d1_out = d1;
+  *g_out = g;
+}
+
+// Per-path contributions from the terminal values of the trajectories.
+__device__ __forceinline__ void contribute(const GInst& I, float S, float S_sp, float S_sm, float S_tm, K32* acc) {
+  const int call = I.payoff == kCall;
+  const float p0 = pay(S, I.K, call);
+  acc[0].add(p0);
+  acc[1].add(p0 * p0);
+  float d1, g;
+  diffs(S, S * (1.0f + I.u), S * (1.0f - I.u), 2.0f * I.u, 0.0f, I.K, call, &d1, &g);
+  acc[2].add(d1);
+  acc[3].add(g);
+  acc[4].add(pay(S_sp, I.K, call) - pay(S_sm, I.K, call));
+  const float pt = pay(S_tm, I.K, call);
+  acc[5].add(pt - p0);
+  acc[6].add(pt);
+  const float sp = S * I.erp, sm = S * I.erm;
+  float dr, gr;
+  diffs(S, sp, sm, I.sh2, 0.0f, I.K, call, &dr, &gr);
+  acc[7].add(dr);
+  acc[8].add(pay(sm, I.K, call));
+}
+
+__device__ void path_gbm(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
+                         K32* acc) {
+  PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
+  K32 w{0.0f, 0.0f};
+  for (uint64_t k = 0; k < I.steps; ++k) w.add(normal_f32(g, c, zs, err));
+  const float W = w.s - w.c;
+  float S[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) S[t] = I.s0 * expf(fmaf(I.diff[t], W, I.kdrift[t]));
+  contribute(I, S[0], S[1], S[2], S[3], acc);
+}
+
+__device__ void merton_pass(const GInst& I, uint64_t p, uint64_t thr, const SamplerCtx& c, const ZigShared& zs,
+                            unsigned& err, float* W, float* J) {
+  PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
+  K32 w{0.0f, 0.0f};
+  float jumps = 0.0f;
+  for (uint64_t k = 0; k < I.steps; ++k) {
+    w.add(normal_f32(g, c, zs, err));
+    if ((g.next() >> 11) < thr) jumps += fmaf(I.sigma_j, normal_f32(g, c, zs, err), I.mu_j);
+  }
+  *W = w.s - w.c;
+  *J = jumps;
+}
+
+__device__ void path_merton(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
+                            K32* acc) {
+  float W, J;
+  merton_pass(I, p, I.jthr[0], c, zs, err, &W, &J);
+  float S[4];
+#pragma unroll
+  for (int t = 0; t < 3; ++t) S[t] = I.s0 * expf(fmaf(I.diff[t], W, I.kdrift[t]) + J);
+  if (I.theta_pass) {
+    float W2, J2;
+    merton_pass(I, p, I.jthr[1], c, zs, err, &W2, &J2);
+    S[3] = I.s0 * expf(fmaf(I.diff[3], W2, I.kdrift[3]) + J2);
+  } else {
+    S[3] = S[0];
+  }
+  contribute(I, S[0], S[1], S[2], S[3], acc);
+}
+
+__device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
+                            K32* acc) {
+  PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
+  float v[4];
+  K32 lg[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    v[t] = I.hv0[t];
+    lg[t] = K32{0.0f, 0.0f};
+  }
+  for (uint64_t k = 0; k < I.steps; ++k) {
+    const float dw1 = normal_f32(g, c, zs, err);
+    const float dz = normal_f32(g, c, zs, err);
+    const float dw2 = fmaf(I.hrho, dw1, I.hrho_comp * dz);
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+      const float vp = fmaxf(v[t], 0.0f);
+      const float sv = sqrtf(vp);
+      v[t] += fmaf(I.hkdt[t], I.htheta - vp, I.hxsdt[t] * sv * dw2);
+      lg[t].add(fmaf(I.hnhdt[t], vp, I.hmudt[t]) + sv * I.hsdt[t] * dw1);
+    }
+  }
+  float S[4];
+#pragma unroll
+  for (int t = 0; t < 4; ++t) S[t] = I.s0 * expf(lg[t].s - lg[t].c);
+  contribute(I, S[0], S[1], S[2], S[3], acc);
+}
+
+__global__ void __launch_bounds__(256) k_greeks(const GreeksLaunch g) {
+  __shared__ ZigShared zs;
+  __shared__ unsigned long long item_s;
+  zig_stage(zs, g.tabs, false);
+  const SamplerCtx c{g.tabs, g.tabs->r32, g.tabs->r};
+  unsigned err = 0;
+  for (;;) {
+    if (threadIdx.x == 0) item_s = atomicAdd(g.counter, 1ull);
+    __syncthreads();
+    const unsigned long long item = item_s;
+    __syncthreads();  // item_s is rewritten next round
+    if (item >= g.total_items) break;
+    const GInst& I = g.inst[g.item_inst[item]];
+    const uint64_t lo = (item - I.item_begin) * I.chunk;
+    uint64_t hi = lo + I.chunk;
+    if (hi > I.n_paths) hi = I.n_paths;
+    K32 acc[kGreekAcc];
+#pragma unroll
+    for (int j = 0; j < kGreekAcc; ++j) acc[j] = K32{0.0f, 0.0f};
+    for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+      if (I.model == kGbm)
+        path_gbm(I, p, c, zs, err, acc);
+      else if (I.model == kHeston)
+        path_heston(I, p, c, zs, err, acc);
+      else
+        path_merton(I, p, c, zs, err, acc);
+    }
+#pragma unroll
+    for (int j = 0; j < kGreekAcc; j += 2) {
+      const double a = (double)(acc[j].s - acc[j].c);
+      const double b = j + 1 < kGreekAcc ? (double)(acc[j + 1].s - acc[j + 1].c) : 0.0;
+      double tmp[2];
+      block_sum2_store(a, b, tmp);  // thread 0 receives the block totals
+      if (threadIdx.x == 0) {
+        g.item_part[item * kGreekAcc + j] = tmp[0];
+        if (j + 1 < kGreekAcc) g.item_part[item * kGreekAcc + j + 1] = tmp[1];
+      }
+    }
+  }
+  if (err) atomicOr(g.err, err);
+}
+
+// One thread per instance: add its items' partials in order.
+__global__ void k_greeks_finish(const GreeksLaunch g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= g.n_inst) return;
+  const GInst& I = g.inst[i];
+  const uint64_t items = (I.n_paths + I.chunk - 1) / I.chunk;
+  double s[kGreekAcc] = {0};
+  for (uint64_t it = 0; it < items; ++it)
+    for (int j = 0; j < kGreekAcc; ++j) s[j] += g.item_part[(I.item_begin + it) * kGreekAcc + j];
+  for (int j = 0; j < kGreekAcc; ++j) g.inst_sums[(uint64_t)i * kGreekAcc + j] = s[j];
+}
+
+}  // namespace
+
+void launch_greeks_batch(const GreeksLaunch& g, cudaStream_t st) {
+  int dev = 0, sms = 152, per_sm = 2;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_greeks, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 2;
+  uint64_t blocks = (uint64_t)sms * per_sm;
+  if (blocks > g.total_items) blocks = g.total_items ? g.total_items : 1;
+  cudaMemsetAsync(g.counter, 0, sizeof(unsigned long long), st);
+  k_greeks<<<(unsigned)blocks, 256, 0, st>>>(g);
+  k_greeks_finish<<<(g.n_inst + 127) / 128, 128, 0, st>>>(g);
+}
+
+}  // namespace stocha

@@ -58,13 +58,24 @@ void make_stream_spec_state(u128 state, u128 inc, u128 block, StreamSpec* ss);
 void pcg_seed(u128 seed, u128* state, u128* inc);
 void pcg_advance(u128* state, u128 inc, u128 delta);
 
+// u < p for u = (draw >> 11) * 2^-53  <=>  (draw >> 11) < unit_threshold(p)
+uint64_t unit_threshold(double p);
+
 // Peak-rate microbenchmarks (peaks.cu).
 double measure_peak(int kind, cudaStream_t st);
 
 // Rust f64 Display (shortest round-trip digits, no exponent).
 std::string rust_f64(double v);
 
-// Model validation with the reference's messages; fills the launch constants.
-int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128* block);
+// Model validation with the reference's messages (check=false skips the
+// range checks, as greeks_fd does, lib.rs:958-1040); fills the launch
+// constants.
+int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128* block, bool check = true);
+// Enqueues a fused pricing launch: sums_dev receives {sum, sum of squares}
+// of the payoff per asset.  aux4: payoff parameters (pathwise estimators).
+int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precision, int payoff, double strike,
+                 const double* aux4, bool check, double* sums_dev, int* nvals);
+// Enqueues a launch writing the terminal price of every path (FP64).
+int terminal_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, double* out_dev);
 
 }  // namespace stocha

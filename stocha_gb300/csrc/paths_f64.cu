@@ -22,9 +22,35 @@ __device__ __forceinline__ double payoff_f64(double s, double k, int kind) {
   return kind == kCall ? fmax(s - k, 0.0) : fmax(k - s, 0.0);
 }
 
+// Payoff of a fused launch, including the pathwise estimators of
+// greeks.rs:387-418 with the reference's expression order.
+__device__ __forceinline__ double launch_payoff(const PathLaunch& a, double s) {
+  const double k = a.strike;
+  switch (a.payoff) {
+    case kCall:
+    case kPut:
+      return payoff_f64(s, k, a.payoff);
+    case kPwDeltaCall:
+      return s > k ? 1.0 * s / a.aux[0] : 0.0;
+    case kPwDeltaPut:
+      return s < k ? -1.0 * s / a.aux[0] : 0.0;
+    default: {
+      const bool call = a.payoff == kPwVegaCall;
+      if (call ? !(s > k) : !(s < k)) return 0.0;
+      const double s0 = a.aux[0], r = a.aux[1], sigma = a.aux[2], t = a.aux[3];
+      const double log_return = log(s / s0);
+      return (call ? 1.0 : -1.0) * s * (log_return - (r + 0.5 * sigma * sigma) * t) / sigma;
+    }
+  }
+}
+
 // Row-major (or time-major) store of one path value.
 __device__ __forceinline__ void store64(const PathLaunch& a, uint64_t lrow, uint64_t step, uint64_t width,
                                         uint64_t col, double v) {
+  if (a.terminal_only) {
+    if (step == a.steps) a.out_f64[lrow * width + col] = v;
+    return;
+  }
   if (a.time_major)
     a.out_f64[(step * width + col) * a.rows + lrow] = v;
   else
@@ -54,7 +80,7 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
       if (kStore) store64(a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
-      double p = payoff_f64(x, a.strike, a.payoff);
+      double p = launch_payoff(a, x);
       acc += p;
       acc2 += p * p;
     }
@@ -103,7 +129,7 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
     if (!kStore) {
 #pragma unroll
       for (int i = 0; i < na; ++i) {
-        double p = payoff_f64(sv[i], a.strike, a.payoff);
+        double p = launch_payoff(a, sv[i]);
         acc[i] += p;
         acc2[i] += p * p;
       }
@@ -185,7 +211,7 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
       }
     }
     if (!kStore) {
-      double p = payoff_f64(x, a.strike, a.payoff);
+      double p = launch_payoff(a, x);
       acc += p;
       acc2 += p * p;
     }
@@ -222,7 +248,7 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
       if (kStore) store64(a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
-      double p = payoff_f64(x, a.strike, a.payoff);
+      double p = launch_payoff(a, x);
       acc += p;
       acc2 += p * p;
     }

@@ -125,6 +125,34 @@ def test_rng_seed_state_matches_oracle(stocha, oracle):
         assert f'"state":{st},' in js and f'"increment":{inc}}}' in js
 
 
+def test_greeks_validation_messages(stocha):
+    gbm = {"s0": 100.0, "r": 0.05, "sigma": 0.2, "t": 1.0}
+    fd = stocha.greeks_fd
+    cases = [  # reference tests/test_greeks.py validation + lib.rs messages
+        (lambda: fd("invalid", gbm, "call", 100.0, 1000, 10, ["delta"]),
+         "Unknown model: 'invalid'. Supported: gbm, heston, merton"),
+        (lambda: fd("gbm", gbm, "call", 100.0, 1000, 10, ["invalid"]),
+         "Unknown greek: 'invalid'. Supported: delta, gamma, vega, theta, rho"),
+        (lambda: fd("gbm", gbm, "binary", 100.0, 1000, 10, ["delta"]),
+         "Unknown payoff: 'binary'. Supported: 'call', 'put', or a callable"),
+        (lambda: fd("gbm", gbm, 3.5, 100.0, 1000, 10, ["delta"]), "payoff must be 'call', 'put', or a callable"),
+        (lambda: fd("gbm", {"s0": 100.0, "sigma": 0.2, "t": 1.0}, "call", 100.0, 1000, 10, ["delta"]),
+         "Missing required param: 'r'"),
+        (lambda: fd("heston", dict(gbm, v0=0.04, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7, scheme="x"), "call", 100.0,
+                    1000, 10, ["delta"]), "scheme must be 'euler' or 'qe'"),
+        (lambda: stocha.greeks_pathwise(-1.0, 0.05, 0.2, 1.0, 100.0, True, 1000, 10, ["delta"]),
+         "s0 must be positive"),
+        (lambda: stocha.greeks_pathwise(100.0, 0.05, 0.2, 1.0, 100.0, True, 0, 10, ["delta"]),
+         "n_paths and n_steps must be positive"),
+        (lambda: stocha.greeks_pathwise(100.0, 0.05, 0.2, 1.0, 100.0, True, 1000, 10, ["gamma"]),
+         "Pathwise method only supports 'delta' and 'vega', got 'gamma'"),
+    ]
+    for fn, msg in cases:
+        with pytest.raises(ValueError) as ei:
+            fn()
+        assert str(ei.value) == msg
+
+
 def test_lsmc_validation_messages(stocha):
     f = stocha.lsmc_american_option
     cases = [
