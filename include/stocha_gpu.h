@@ -129,6 +129,19 @@ int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t 
 int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
                         double strike, double rate, double* out_dev);
 
+/* Fused pricing without any device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc: a host application
+ * that owns all device memory, or a request path that must never reach the
+ * allocator.  Same kernels and output as stocha_price_device (out_dev: 2 *
+ * n_assets doubles of raw payoff sums, caller-owned device memory), on the
+ * caller's cudaStream_t; scratch, tables and status live in static device
+ * arrays of the library (1 MiB of scratch: at most 4 assets).  Synchronous:
+ * waits for `stream` and reports device-check failures.  The first call on a
+ * device sets up its arrays (make it before any stream capture); calls that
+ * overlap on the GPU share the arrays and race. */
+int stocha_price_noalloc(const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff, double strike,
+                         double* sums_dev, void* stream);
+
 /* ----------------------------------------------------------------- LSMC */
 /* replaces #[pyfunction] lsmc_american_option, src/lib.rs:854-918 ->
  * finance/lsmc.rs:25 lsmc_american_option.  FP64 paths (the reference's),

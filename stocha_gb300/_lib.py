@@ -100,6 +100,7 @@ SIGNATURES = [
                                  c_dbl, c_u64, c_u64, P_charp, c_u64, c_u64, c_dbl, c_i32, P_dbl]),
     ("stocha_greeks_pathwise", c_i32, [c_void_p] + [c_dbl] * 5 + [c_i32, c_u64, c_u64, P_charp, c_u64, c_u64, P_dbl]),
     ("stocha_greeks_batch", c_i32, [c_void_p, ctypes.POINTER(StochaGreeksInstance), c_u64, c_i32, P_dbl]),
+    ("stocha_price_noalloc", c_i32, [ctypes.POINTER(StochaModel), c_u64, c_i32, c_i32, c_dbl, c_void_p, c_void_p]),
     ("stocha_debug_zig_thresholds", c_i32, [P_u64]),
     ("stocha_measure_peak", c_i32, [c_void_p, c_i32, P_dbl]),
 ]

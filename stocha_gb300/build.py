@@ -32,6 +32,7 @@ CUDA_UNITS = {
     "greeks.cu": [],
     "batch.cu": [],
     "peaks.cu": [],
+    "noalloc.cu": [],
 }
 HOST_UNITS = ["api.cpp", "rng_host.cpp", "lsmc_host.cpp", "greeks_host.cpp", "batch_host.cpp", "serve.cpp"]
 

@@ -128,6 +128,8 @@ std::string u128_str(u128 v) {
 
 }  // namespace
 
+void fill_zig_tables(ZigTables* t) { build_tables(t); }
+
 int set_error(int code, const std::string& msg) {
   g_err = msg;
   return code;

@@ -58,6 +58,9 @@ void make_stream_spec_state(u128 state, u128 inc, u128 block, StreamSpec* ss);
 void pcg_seed(u128 seed, u128* state, u128* inc);
 void pcg_advance(u128* state, u128 inc, u128 delta);
 
+// The ziggurat tables as the kernels read them (thresholds derived on the host).
+void fill_zig_tables(ZigTables* t);
+
 // u < p for u = (draw >> 11) * 2^-53  <=>  (draw >> 11) < unit_threshold(p)
 uint64_t unit_threshold(double p);
 
