@@ -136,6 +136,113 @@ def cpu_baseline(threads: int, sample_paths: int):
     return 3 * sample_paths * STEPS / dt
 
 
+def greeks_instances(n=512, seed=20261203):
+    """The 512 seeded Greeks instances: s0~U[80,120], sigma~U[.1,.5],
+    r~U[0,.06], t~U[.1,2], K=s0*U[.8,1.2], model uniform over gbm / heston
+    (kappa=2, theta=.04, xi=.3, rho=-.7, v0=sigma^2) / merton (lambda=1,
+    mu_j=-.05, sigma_j=.1), n_paths=10^U[4,6], steps in {12, 52, 252}, call."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        s0 = float(rng.uniform(80, 120))
+        d = dict(model=["gbm", "heston", "merton"][int(rng.integers(0, 3))], s0=s0,
+                 sigma=float(rng.uniform(0.1, 0.5)), r=float(rng.uniform(0.0, 0.06)), t=float(rng.uniform(0.1, 2.0)))
+        d["strike"] = s0 * float(rng.uniform(0.8, 1.2))
+        d["n_paths"] = int(round(10 ** rng.uniform(4, 6)))
+        d["steps"] = int(rng.choice([12, 52, 252]))
+        d["payoff"] = "call"
+        d["seed"] = 42
+        if d["model"] == "heston":
+            d.update(v0=d["sigma"] ** 2, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7)
+        if d["model"] == "merton":
+            d.update(lambda_=1.0, mu_j=-0.05, sigma_j=0.1)
+        out.append(d)
+    return out
+
+
+def bench_extras(stocha, torch, cores, skip_cpu):
+    """Configurations 1, 3 and 4 beside the headline (each a few seconds)."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    res = {}
+    # -- config 1: GBM FP64, 1e5 x 252, seed 42 (the reference's own benchmark case)
+    steps1, n1 = 252, 100_000
+    m = stocha.model_struct("gbm", dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0), steps1, n1)
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    buf = torch.empty((n1, steps1 + 1), dtype=torch.float64, device="cuda")
+    for _ in range(3):
+        _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), 42, _lib.FP64, ctypes.c_void_p(buf.data_ptr())))
+    _lib.check(lib.stocha_ctx_sync(None))
+    k = 20
+    t0 = time.perf_counter()
+    for _ in range(k):
+        _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), 42, _lib.FP64, ctypes.c_void_p(buf.data_ptr())))
+    _lib.check(lib.stocha_ctx_sync(None))
+    dev_s = (time.perf_counter() - t0) / k
+    stocha.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        stocha.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42)
+    e2e_s = (time.perf_counter() - t0) / 5
+    c1 = {"workload": "gbm fp64 1e5 paths x 252 steps, seed 42", "value": n1 * steps1 / dev_s,
+          "unit": "path-steps/s", "e2e": {"value": n1 * steps1 / e2e_s, "unit": "path-steps/s",
+                                          "d2h_bytes_per_step": n1 * (steps1 + 1) * 8}}
+    if not skip_cpu:
+        O.gbm(100.0, 0.05, 0.2, 1.0, steps1, 20_000, seed=42, threads=cores, gather=True)
+        t0 = time.perf_counter()
+        O.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42, threads=cores, gather=True)
+        c1["cpu_baseline"] = {"value": n1 * steps1 / (time.perf_counter() - t0), "cores": cores, "kind": "port"}
+    res["config1_gbm_fp64"] = c1
+    del buf
+    # -- config 3: LSMC American put, s0=k=100, r=.05, sigma=.2, t=1, 50 steps, degree 3
+    c3 = {"workload": "lsmc put s0=k=100 r=.05 sigma=.2 t=1 steps=50 deg=3 seed=42"}
+    for n in (50_000, 4_000_000):
+        row = {}
+        for prec in ("fp64", "fp32"):
+            stocha.lsmc_american_option(100.0, 100.0, 0.05, 0.2, 1.0, 50, n, precision=prec)
+            t0 = time.perf_counter()
+            reps = 5 if n < 1e6 else 3
+            for _ in range(reps):
+                p, se = stocha.lsmc_american_option(100.0, 100.0, 0.05, 0.2, 1.0, 50, n, precision=prec)
+            row[prec] = {"price": p, "std_err": se, "ms": 1e3 * (time.perf_counter() - t0) / reps,
+                         "path_steps_per_s": n * 50 / ((time.perf_counter() - t0) / reps)}
+        row["fp32_minus_fp64"] = row["fp32"]["price"] - row["fp64"]["price"]
+        c3[str(n)] = row
+    if not skip_cpu:
+        t0 = time.perf_counter()
+        p, se = O.lsmc(100.0, 100.0, 0.05, 0.2, 1.0, 50, 50_000, seed=42, threads=cores)
+        c3["cpu_baseline_50000"] = {"price": p, "std_err": se, "ms": 1e3 * (time.perf_counter() - t0),
+                                    "cores": cores, "kind": "port",
+                                    "note": "paths on all cores, backward sweep single-threaded as in lsmc.rs"}
+        c3["50000"]["fp64_minus_cpu_qr"] = c3["50000"]["fp64"]["price"] - p
+    res["config3_lsmc"] = c3
+    # -- config 4: 512 Greeks instances, one persistent FP32 launch
+    insts = greeks_instances()
+    draw_steps = sum(d["n_paths"] * d["steps"] for d in insts)
+    stocha.greeks_batch(insts[:8])
+    t0 = time.perf_counter()
+    g32 = stocha.greeks_batch(insts, precision="fp32")
+    dt = time.perf_counter() - t0
+    sample = list(range(0, 512, 32))
+    g64 = stocha.greeks_batch([insts[i] for i in sample], precision="fp64")
+    rel = np.abs(g32[sample][:, [0, 2, 3, 4, 5, 6]] - g64[:, [0, 2, 3, 4, 5, 6]]) / np.maximum(
+        np.abs(g64[:, [0, 2, 3, 4, 5, 6]]), 1e-3)
+    names = ["price", "delta", "gamma", "vega", "theta", "rho"]
+    res["config4_greeks_batch"] = {
+        "instances": 512, "seconds": dt, "draw_steps": draw_steps,
+        "scenario_path_steps_per_s": 7 * draw_steps / dt, "draw_steps_per_s": draw_steps / dt,
+        "fp32_vs_fp64_rel_err_median": dict(zip(names, np.median(rel, axis=0).tolist())),
+        "fp32_vs_fp64_rel_err_max": dict(zip(names, np.max(rel, axis=0).tolist())),
+        "fp64_sample": f"{len(sample)} instances (every 32nd) revalued scenario by scenario in FP64"}
+    return res
+
+
 def host_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -301,6 +408,10 @@ def run_ours(args, rank, world):
                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8 * N_PATHS * (STEPS + 1) * 5}
         fp64["fp32_fused_speedup"] = value / fp64["value"]
 
+    extras = {}
+    if rank == 0 and not args.skip_extras:
+        extras = bench_extras(stocha, torch, host_cores(), args.skip_cpu)
+
     cpu = None
     if rank == 0 and not args.skip_cpu:
         cores = host_cores()
@@ -329,6 +440,7 @@ def run_ours(args, rank, world):
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -344,6 +456,7 @@ def main():
     ap.add_argument("--skip-e2e64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-extras", action="store_true", help="only the headline workload")
     ap.add_argument("--paths", type=int, default=N_PATHS, help="paths per model (profiling cases)")
     args = ap.parse_args()
     globals()["N_PATHS"] = args.paths

@@ -102,6 +102,7 @@ SIGNATURES = [
     ("stocha_greeks_batch", c_i32, [c_void_p, ctypes.POINTER(StochaGreeksInstance), c_u64, c_i32, P_dbl]),
     ("stocha_price_noalloc", c_i32, [ctypes.POINTER(StochaModel), c_u64, c_i32, c_i32, c_dbl, c_void_p, c_void_p]),
     ("stocha_debug_zig_thresholds", c_i32, [P_u64]),
+    ("stocha_debug_exp", c_i32, [c_void_p, P_dbl, P_dbl, c_u64]),
     ("stocha_measure_peak", c_i32, [c_void_p, c_i32, P_dbl]),
 ]
 

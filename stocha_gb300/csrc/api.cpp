@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "exp_table.inc"
 #include "host_common.h"
 #include "ziggurat_table.inc"
 
@@ -66,6 +67,8 @@ void build_tables(ZigTables* t) {
   }
   t->r = STOCHA_ZIG_R_HEX;
   t->r32 = (float)t->r;
+  static const double E2[128] = STOCHA_EXP2_TAB_INIT;
+  for (int j = 0; j < 128; ++j) t->exp2tab[j] = E2[j];
 }
 
 // Brown's arbitrary-stride LCG jump (rand_pcg advance, pcg64.rs:41-43):
@@ -575,6 +578,22 @@ int stocha_measure_peak(stocha_ctx* ctx, int32_t kind, double* ops_per_s) {
   if (v <= 0) return set_error(STOCHA_ERR_NOMEM, "peak benchmark allocation failed");
   *ops_per_s = v;
   return STOCHA_OK;
+}
+
+int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n) {
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  if (n == 0) return STOCHA_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if ((rc = ensure_buf(ctx, ctx->aux, 2 * n * sizeof(double)))) return rc;
+  double* d = (double*)ctx->aux.ptr;
+  if ((rc = begin_call(ctx))) return rc;
+  STOCHA_CUDA(cudaMemcpyAsync(d, x, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  launch_debug_exp(d, d + n, n, ctx->d_tabs, ctx->stream);
+  STOCHA_CUDA(cudaGetLastError());
+  STOCHA_CUDA(cudaMemcpyAsync(y, d + n, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish_call(ctx);
 }
 
 int stocha_debug_zig_thresholds(uint64_t* thr256) {

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
     for (uint64_t k = 1; k <= a.steps; ++k) {
       double z = normal_f64(s, c, zs, err);
       if (neg) z = -z;
-      x *= exp(drift + diffusion * z);
+      x = mul_exp(x, fma(diffusion, z, drift), zs);
       if (kStore) store64(a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
         double eps = 0.0;
 #pragma unroll
         for (int m = 0; m <= i; ++m) eps += a.multi.L[i * kMaxAssets + m] * z[m];
-        sv[i] *= exp(a.multi.drift[i] + a.multi.diffusion[i] * eps);
+        sv[i] = mul_exp(sv[i], fma(a.multi.diffusion[i], eps, a.multi.drift[i]), zs);
         if (kStore) store64(a, lrow, k, na, i, sv[i]);
       }
     }
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
         double v_plus = fmax(v, 0.0);
         double sqrt_v = sqrt(v_plus);
         v += h.kappa * (h.theta - v_plus) * h.dt + h.xi * sqrt_v * h.sqrt_dt * dw2;
-        x *= exp((h.mu - 0.5 * v_plus) * h.dt + sqrt_v * h.sqrt_dt * dw1);
+        x = mul_exp(x, (h.mu - 0.5 * v_plus) * h.dt + sqrt_v * h.sqrt_dt * dw1, zs);
         if (kStore) store64(a, lrow, k, 1, 0, x);
       }
     } else {
@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
         double z_j = normal_f64(s, c, zs, err);
         jump_return = M.mu_j + M.sigma_j * z_j;
       }
-      x *= exp(diffusion_return + jump_return);
+      x = mul_exp(x, diffusion_return + jump_return, zs);
       if (kStore) store64(a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
@@ -255,6 +255,14 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
   }
   if (!kStore) block_sum2_store(acc, acc2, a.partials + 2 * blockIdx.x);
   if (err) atomicOr(a.err, err);
+}
+
+__global__ void k_debug_exp(const double* __restrict__ x, double* __restrict__ y, uint64_t n,
+                            const ZigTables* tabs) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, tabs, true);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    y[i] = mul_exp(1.0, x[i], zs);
 }
 
 __global__ void k_reduce_partials(const double* __restrict__ partials, int nblocks, int nvals,
@@ -318,6 +326,10 @@ int launch_paths_f64(const PathLaunch& L, cudaStream_t st) {
       return -1;
   }
   return cudaPeekAtLastError() == cudaSuccess ? g : -1;
+}
+
+void launch_debug_exp(const double* x, double* y, uint64_t n, const ZigTables* tabs, cudaStream_t st) {
+  k_debug_exp<<<256, 256, 0, st>>>(x, y, n, tabs);
 }
 
 void launch_reduce_partials(const double* partials, int nblocks, int nvals, double* out, cudaStream_t st) {

@@ -160,3 +160,33 @@ def test_config2_prefix_rows_full_size(stocha, oracle):
     got = stocha.merton_jump_diffusion(100, 0.05, 0.2, 1.0, -0.05, 0.1, 1.0, 252, n, seed=42)
     want = oracle.merton(100, 0.05, 0.2, 1.0, -0.05, 0.1, 1.0, 252, k, seed=42)
     assert _rel(got[:k], want) <= PATH_RTOL
+
+
+def test_table_exp_accuracy(stocha):
+    """The FP64 path kernels' exponential (table-driven, 2^(j/128) table plus
+    a degree-5 polynomial) against numpy's exp: <= 3 ulp over the working
+    range, exact special values, subnormal and overflow results."""
+    import ctypes
+
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(7)
+    x = np.concatenate([
+        rng.uniform(-1, 1, 200_000), rng.uniform(-40, 40, 200_000), rng.uniform(-699.9, 699.9, 100_000),
+        rng.normal(0, 1e-3, 50_000),
+        np.array([0.0, -0.0, 1e-300, -1e-300, 0.5, 1.0, -1.0, 699.99, -699.99, 700.0, -700.0, 709.7, 710.0, -708.5,
+                  -745.0, -800.0, np.inf, -np.inf, np.nan]),
+    ])
+    y = np.empty_like(x)
+    P = ctypes.POINTER(ctypes.c_double)
+    _lib.check(lib.stocha_debug_exp(None, x.ctypes.data_as(P), y.ctypes.data_as(P), x.size))
+    want = np.exp(x)
+    fin = np.isfinite(want) & (want > np.finfo(float).tiny)
+    ulp = np.abs(y[fin] - want[fin]) / np.spacing(want[fin])
+    assert ulp.max() <= 3.0, ulp.max()
+    assert y[x == 0.0].tolist() == [1.0, 1.0]
+    assert np.isinf(y[x == np.inf]).all() and (y[x == -np.inf] == 0).all() and np.isnan(y[np.isnan(x)]).all()
+    assert np.isinf(y[x == 710.0]).all()
+    sub = (want > 0) & (want < np.finfo(float).tiny)
+    assert np.allclose(y[sub], want[sub], rtol=1e-12, atol=2 * np.spacing(0.0))
