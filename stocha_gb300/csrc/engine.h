@@ -66,6 +66,8 @@ struct PathLaunch {
   double aux[4];  // payoff parameters (pathwise estimators: s0, r, sigma, t)
   uint64_t row_begin, rows, steps, base_paths;
   int model;
+  int flat_grid;  // FP32 kernels: one row per thread and no grid cap (blocks retire
+                  // early, so work on higher-priority streams gets SMs sooner)
   GbmK gbm;
   HestonK heston;
   MertonK merton;

@@ -81,4 +81,22 @@ int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precis
 // Enqueues a launch writing the terminal price of every path (FP64).
 int terminal_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, double* out_dev);
 
+// One LSMC American option (lsmc.rs:4-14) as a job over caller-owned device
+// buffers: the path array and the sweep scratch.
+struct LsmcJob {
+  double s0, k, r, sigma, t;
+  uint64_t steps, n_paths, deg, seed;
+  int is_put, precision;
+};
+// Argument checks with the reference's messages (lib.rs:885-903).
+int lsmc_validate(const LsmcJob& j);
+void lsmc_footprint(const LsmcJob& j, int sms, size_t* path_bytes, size_t* scratch_bytes);
+// Enqueues paths and sweep on st; *result_dev receives the device address of
+// {mean of discounted cash flows, sum of squared deviations}.  flat: path
+// launch with one path per thread (see PathLaunch::flat_grid).
+int lsmc_enqueue(const LsmcJob& j, int sms, void* paths, void* scratch, const ZigTables* tabs, unsigned* err,
+                 bool flat, cudaStream_t st, const double** result_dev);
+// Price and standard error from the two device results (lsmc.rs:100-114).
+void lsmc_estimate(const LsmcJob& j, const double* res2, double* price, double* std_err);
+
 }  // namespace stocha

@@ -243,7 +243,7 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, b, 0) != cudaSuccess || per_sm < 1) per_sm = 2;
   uint64_t g = (L.rows + b - 1) / b;
   const uint64_t cap = (uint64_t)sms * per_sm;
-  if (g > cap) g = cap;
+  if (g > cap && !L.flat_grid) g = cap;
   if (g < 1) g = 1;
   dim3 G((unsigned)g), B(b);
   switch (L.model) {

@@ -80,3 +80,18 @@ def test_lsmc_fp32_paths(stocha, n):
     if n >= 1_000_000:
         assert abs(p32 - p64) <= FP32_RTOL * p64, (p32, p64)
     assert abs(se32 - se64) <= 1e-3 * se64
+
+
+@pytest.mark.parametrize("n,prec", [(600_000, "fp64"), (600_000, "fp32"), (30_000, "fp32")])
+def test_lsmc_sweep_forms(stocha, oracle, n, prec):
+    """Above 2^19 paths the sweep runs as one launch per step, below as one
+    cluster launch: both against the oracle (FP64: same solver, LSMC_SAME_SOLVER_RTOL;
+    FP32: a tenth of a standard error)."""
+    kw = dict(s0=100.0, k=100.0, r=0.05, sigma=0.2, t=1.0, steps=50, n_paths=n, seed=11)
+    p, se = stocha.lsmc_american_option(**kw, precision=prec)
+    pq, seq = oracle.lsmc(100.0, 100.0, 0.05, 0.2, 1.0, 50, n, seed=11, solver="normal")
+    if prec == "fp64":
+        assert abs(p - pq) <= LSMC_SAME_SOLVER_RTOL * pq, (p, pq)
+        assert abs(se - seq) <= 1e-8 * seq
+    else:
+        assert abs(p - pq) <= 0.1 * seq, (p, pq, seq)
