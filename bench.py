@@ -18,6 +18,10 @@ One "step" = one pass of all three models.  Path-steps per step = 3 * 2.52e8
           generator alone (stocha_measure_peak kind 3).
   cpu_baseline  the C++ oracle (restatement of the reference's Rayon
           algorithm) on the host cores, bounded sample.
+  config5_serving  20 000 pricing / Greeks / LSMC requests, Poisson arrivals
+          at 2000/s, through stocha_gb300.Server (40 GB budget): p50/p99
+          latency overall and for requests of <= 1e5 paths, requests/s, and
+          the per-request error of a sample against the FP64 plain form.
 
 --impl reference runs the C++ oracle (the reference itself is Rust and cannot
 be built here) on all host cores for the same workload, each step a sample of
@@ -38,6 +42,9 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# the serving loop runs many concurrent streams: give them hardware queues of
+# their own (read when the CUDA context is created, i.e. before torch starts it)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 N_PATHS = 1_000_000  # --paths overrides (small cases for profiling only)
 STEPS = 252
@@ -162,6 +169,117 @@ def greeks_instances(n=512, seed=20261203):
     return out
 
 
+def serving_requests(n=20_000, seed=20261204, rate=2000.0):
+    """The serving mix: each request draws model, parameters and payoff from
+    the Greeks-instance distributions (s0~U[80,120], sigma~U[.1,.5],
+    r~U[0,.06], t~U[.1,2], K=s0*U[.8,1.2], model uniform over gbm / heston /
+    merton with the fixed model parameters), kind uniform over price and
+    greeks, call/put uniform; with probability 0.2 it is an LSMC put (degree
+    3) instead.  n_paths = 10^U[4, log10 2e6], steps in {12, 50, 252}, seeds
+    drawn per request; Poisson arrivals at `rate` per second."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for _ in range(n):
+        s0 = float(rng.uniform(80, 120))
+        d = dict(s0=s0, sigma=float(rng.uniform(0.1, 0.5)), r=float(rng.uniform(0.0, 0.06)),
+                 t=float(rng.uniform(0.1, 2.0)))
+        d["strike"] = s0 * float(rng.uniform(0.8, 1.2))
+        d["n_paths"] = int(round(10 ** rng.uniform(4, math.log10(2e6))))
+        d["steps"] = int(rng.choice([12, 50, 252]))
+        d["seed"] = int(rng.integers(1 << 63))
+        if rng.random() < 0.2:
+            d.update(kind="lsmc", payoff="put", poly_degree=3)
+        else:
+            d["model"] = ["gbm", "heston", "merton"][int(rng.integers(0, 3))]
+            d["kind"] = ["price", "greeks"][int(rng.integers(0, 2))]
+            d["payoff"] = ["call", "put"][int(rng.integers(0, 2))]
+            if d["model"] == "heston":
+                d.update(v0=d["sigma"] ** 2, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7)
+            if d["model"] == "merton":
+                d.update(lambda_=1.0, mu_j=-0.05, sigma_j=0.1)
+        reqs.append(d)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    return reqs, arrivals
+
+
+def _fp64_plain(stocha, q):
+    """The FP64 plain form (the reference's arithmetic) of one served request:
+    its price, and its five Greeks for a Greeks request."""
+    if q["kind"] == "lsmc":
+        p, se = stocha.lsmc_american_option(q["s0"], q["strike"], q["r"], q["sigma"], q["t"], q["steps"],
+                                            q["n_paths"], is_put=True, poly_degree=q["poly_degree"], seed=q["seed"])
+        return {"price": p}
+    keys = {"gbm": ("s0", "sigma", "t"), "heston": ("s0", "v0", "kappa", "theta", "xi", "rho", "t"),
+            "merton": ("s0", "sigma", "lambda_", "mu_j", "sigma_j", "t")}[q["model"]]
+    params = {k: q[k] for k in keys}
+    params["mu"] = q["r"]
+    p, se = stocha.price_european(q["model"], params, q["strike"], payoff=q["payoff"], steps=q["steps"],
+                                  n_paths=q["n_paths"], seed=q["seed"], precision="fp64", rate=q["r"])
+    out = {"price": p}
+    if q["kind"] == "greeks":
+        params.pop("mu")
+        params["r"] = q["r"]
+        out["greeks"] = stocha.greeks_fd(q["model"], params, q["payoff"], q["strike"], q["n_paths"], q["steps"],
+                                         ["delta", "gamma", "vega", "theta", "rho"], seed=q["seed"], bump_size=0.01)
+    return out
+
+
+def bench_serving(stocha, n=20_000, rate=2000.0, budget=40 << 30, lanes=32, sample=60):
+    """Configuration 5: open-loop serving of the mix; latency, throughput and
+    the error of a sample of requests against the FP64 plain form."""
+    import numpy as np
+    from stocha_gb300.serve import latency_summary
+
+    reqs, arrivals = serving_requests(n, rate=rate)
+    with stocha.Server(budget_bytes=budget, lanes=lanes) as srv:
+        srv.replay(reqs[:64], np.zeros(64))  # warm-up: code paths, graph instantiation
+        t0 = time.perf_counter()
+        res = srv.replay(reqs, arrivals)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    out = latency_summary(res, reqs)
+    lat = np.array([r["t_done"] - r["t_submit"] for r in res]) * 1e3
+    kinds = np.array([q["kind"] for q in reqs])
+    small = np.array([q["n_paths"] <= 100_000 for q in reqs])
+    out["by_kind_p99_ms"] = {f"{k}_{'small' if s else 'large'}": float(np.percentile(lat[(kinds == k) & (small == s)], 99))
+                             for k in ("price", "greeks", "lsmc") for s in (True, False)
+                             if ((kinds == k) & (small == s)).any()}
+    path_steps = sum(q["n_paths"] * q["steps"] for q in reqs)
+    out.update(failed=int(sum(r["status"] != "done" for r in res)), wall_s=wall,
+               offered_req_per_s=rate, path_steps_per_s=path_steps / wall,
+               budget_bytes=budget, peak_bytes=st["peak_bytes"], lanes=lanes, jobs=st["jobs"],
+               batched_requests=st["batched_requests"])
+    # per-request error against the FP64 plain form, on an even sample
+    idx = np.linspace(0, n - 1, sample).astype(int)
+    eu, gk, ls, ls_se = [], [], [], []
+    for i in idx:
+        q, r = reqs[i], res[i]
+        ref = _fp64_plain(stocha, q)
+        d = abs(r["price"] - ref["price"])
+        if q["kind"] == "lsmc":
+            ls.append(d / abs(ref["price"]))
+            ls_se.append(d / r["std_err"])
+            continue
+        eu.append(d / abs(ref["price"]))
+        if "greeks" in ref:  # each Greek relative to max(|greek|, 1% of the price)
+            gk.extend(abs(r["greeks"][k] - v) / max(abs(v), 0.01 * abs(ref["price"])) for k, v in ref["greeks"].items())
+    f = lambda v, fn: float(fn(v)) if v else None
+    out["error_vs_fp64_plain"] = {
+        "sample": int(sample),
+        "european_price_rel_err_max": f(eu, max), "european_price_rel_err_median": f(eu, np.median),
+        "european_price_over_1e-4": int(sum(e > 1e-4 for e in eu)), "european_n": len(eu),
+        "greeks_rel_err_max": f(gk, max), "greeks_rel_err_median": f(gk, np.median),
+        "lsmc_price_rel_err_max": f(ls, max), "lsmc_price_rel_err_median": f(ls, np.median),
+        "lsmc_abs_err_over_std_err_max": f(ls_se, max), "lsmc_n": len(ls),
+        "note": "LSMC: FP32 paths and regression move exercise decisions at near-ties; the difference to the "
+                "FP64 plain form is statistical (a fraction of one standard error)"}
+    out["workload"] = (f"{n} requests, Poisson {rate:.0f}/s; price/greeks on gbm/heston/merton (Greeks-instance "
+                       "distributions) + 20% LSMC puts; n_paths=10^U[4,log10 2e6], steps in {12,50,252}; FP32 forms")
+    return out
+
+
 def bench_extras(stocha, torch, cores, skip_cpu):
     """Configurations 1, 3 and 4 beside the headline (each a few seconds)."""
     import numpy as np
@@ -240,6 +358,8 @@ def bench_extras(stocha, torch, cores, skip_cpu):
         "fp32_vs_fp64_rel_err_median": dict(zip(names, np.median(rel, axis=0).tolist())),
         "fp32_vs_fp64_rel_err_max": dict(zip(names, np.max(rel, axis=0).tolist())),
         "fp64_sample": f"{len(sample)} instances (every 32nd) revalued scenario by scenario in FP64"}
+    # -- config 5: the serving loop
+    res["config5_serving"] = bench_serving(stocha)
     return res
 
 

@@ -32,6 +32,7 @@ extern "C" {
 #define STOCHA_ERR_DEVICE 4   /* a kernel's own check failed (iteration cap) */
 #define STOCHA_ERR_CALLBACK 5 /* a user payoff callback reported failure */
 #define STOCHA_ERR_BUSY 6     /* serving: admission refused (memory budget) */
+#define STOCHA_ERR_TIMEOUT 7  /* serving: a wait ended before the request finished */
 
 #define STOCHA_FP64 0 /* reference arithmetic, exact operation order */
 #define STOCHA_FP32 1 /* FP32 paths, FP64 reductions */
@@ -241,6 +242,68 @@ int stocha_rng_from_state(const char* json, stocha_rng* out);
 /* Raw generator output (no counterpart call in the reference API; used to
  * check the device generator against the reference bit for bit). */
 int stocha_rng_raw_u64(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, uint64_t* out);
+
+/* -------------------------------------------------------------- serving
+ * No counterpart in the reference (its API is one blocking call per
+ * pricing).  A server owns one device-memory budget, a set of CUDA streams
+ * ("lanes": an eighth at the highest stream priority for small pricing and
+ * Greeks batches, a quarter at a middle priority for LSMC jobs, the rest at
+ * the lowest for large pricing and Greeks requests) and a dispatcher thread
+ * that
+ * admits requests as their bytes fit and batches small pricing/Greeks
+ * requests into one launch as they arrive; each request is computed as the
+ * reference's call would be:
+ *   STOCHA_REQ_PRICE   European call/put price and standard error
+ *                      (greeks.rs:322-329 mc_price), FP32 paths
+ *   STOCHA_REQ_GREEKS  greeks_fd with all five Greeks (greeks.rs:330-358),
+ *                      FP32 common-random-number batch
+ *   STOCHA_REQ_LSMC    lsmc_american_option (lsmc.rs:25-115), FP32 paths
+ *                      and FP64 regression; inst.payoff selects put/call,
+ *                      inst.strike is k, inst.r the rate, poly_degree the
+ *                      polynomial degree
+ * Results depend only on the request, never on what else is in flight. */
+#define STOCHA_REQ_PRICE 0
+#define STOCHA_REQ_GREEKS 1
+#define STOCHA_REQ_LSMC 2
+
+typedef struct stocha_server stocha_server;
+
+typedef struct stocha_request {
+  int32_t kind;        /* STOCHA_REQ_* */
+  int32_t poly_degree; /* LSMC: 1..4 */
+  stocha_greeks_instance inst;
+} stocha_request;
+
+typedef struct stocha_result {
+  int32_t status; /* 0 pending, 1 done, -STOCHA_ERR_* if the request failed */
+  int32_t pad;
+  double price, std_err;
+  double greeks[5];                 /* delta gamma vega theta rho (STOCHA_REQ_GREEKS) */
+  double t_submit, t_admit, t_done; /* seconds on the server's clock */
+} stocha_result;
+
+typedef struct stocha_server_counters {
+  uint64_t submitted, completed, failed, jobs, batched_requests;
+  uint64_t budget_bytes, peak_bytes, in_use_bytes;
+  int32_t lanes, high_lanes; /* high_lanes: lanes above the lowest priority */
+} stocha_server_counters;
+
+int stocha_server_create(int32_t device, uint64_t budget_bytes, int32_t lanes, stocha_server** out);
+/* Finishes every submitted request, then releases the server. */
+int stocha_server_destroy(stocha_server* s);
+/* Validates (the reference's messages) and queues a request. */
+int stocha_server_submit(stocha_server* s, const stocha_request* req, uint64_t* ticket);
+int stocha_server_poll(stocha_server* s, uint64_t ticket, stocha_result* out);
+/* timeout_s < 0: wait without limit. */
+int stocha_server_wait(stocha_server* s, uint64_t ticket, double timeout_s, stocha_result* out);
+/* Open-loop load: submits reqs[i] at arrival_s[i] seconds after the call
+ * starts, then waits for all; out[i] is request i's result. */
+int stocha_server_replay(stocha_server* s, const stocha_request* reqs, const double* arrival_s, uint64_t n,
+                         stocha_result* out);
+int stocha_server_stats(stocha_server* s, stocha_server_counters* out);
+/* Diagnostic (no counterpart in the reference): the serving arena's
+ * allocator on a host-only script, see serve.cpp. */
+int stocha_debug_arena(uint64_t capacity, const int64_t* ops, uint64_t n, int64_t* res);
 
 #ifdef __cplusplus
 }

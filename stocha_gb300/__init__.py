@@ -24,6 +24,7 @@ import numpy as np
 
 from . import _lib, _stocha
 from ._stocha import __version__
+from .serve import Server
 
 __all__ = [
     "RNG",
@@ -37,6 +38,7 @@ __all__ = [
     "greeks_batch",
     "price_european",
     "model_struct",
+    "Server",
     "__version__",
 ]
 

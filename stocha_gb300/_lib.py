@@ -20,6 +20,8 @@ STOCHA_ERR_NOMEM = 3
 STOCHA_ERR_DEVICE = 4
 STOCHA_ERR_CALLBACK = 5
 STOCHA_ERR_BUSY = 6
+STOCHA_ERR_TIMEOUT = 7
+REQ_PRICE, REQ_GREEKS, REQ_LSMC = 0, 1, 2
 
 FP64, FP32 = 0, 1
 MODEL_GBM, MODEL_HESTON, MODEL_MERTON, MODEL_MULTI_GBM = 0, 1, 2, 3
@@ -57,6 +59,21 @@ class StochaGreeksInstance(ctypes.Structure):
         [(k, c_dbl) for k in ("s0", "r", "sigma", "t", "v0", "kappa", "theta", "xi", "rho", "lambda_", "mu_j",
                               "sigma_j", "strike", "bump_size")] + \
         [("n_paths", c_u64), ("steps", c_u64), ("seed", c_u64)]
+
+
+class StochaRequest(ctypes.Structure):
+    _fields_ = [("kind", c_i32), ("poly_degree", c_i32), ("inst", StochaGreeksInstance)]
+
+
+class StochaResult(ctypes.Structure):
+    _fields_ = [("status", c_i32), ("pad", c_i32), ("price", c_dbl), ("std_err", c_dbl),
+                ("greeks", c_dbl * 5), ("t_submit", c_dbl), ("t_admit", c_dbl), ("t_done", c_dbl)]
+
+
+class StochaServerCounters(ctypes.Structure):
+    _fields_ = [(k, c_u64) for k in ("submitted", "completed", "failed", "jobs", "batched_requests",
+                                     "budget_bytes", "peak_bytes", "in_use_bytes")] + \
+        [("lanes", c_i32), ("high_lanes", c_i32)]
 
 
 PAYOFF_FN = ctypes.CFUNCTYPE(c_i32, c_void_p, P_dbl, c_u64, P_dbl, ctypes.POINTER(c_u64))
@@ -101,6 +118,15 @@ SIGNATURES = [
     ("stocha_greeks_pathwise", c_i32, [c_void_p] + [c_dbl] * 5 + [c_i32, c_u64, c_u64, P_charp, c_u64, c_u64, P_dbl]),
     ("stocha_greeks_batch", c_i32, [c_void_p, ctypes.POINTER(StochaGreeksInstance), c_u64, c_i32, P_dbl]),
     ("stocha_price_noalloc", c_i32, [ctypes.POINTER(StochaModel), c_u64, c_i32, c_i32, c_dbl, c_void_p, c_void_p]),
+    ("stocha_server_create", c_i32, [c_i32, c_u64, c_i32, ctypes.POINTER(c_void_p)]),
+    ("stocha_server_destroy", c_i32, [c_void_p]),
+    ("stocha_server_submit", c_i32, [c_void_p, ctypes.POINTER(StochaRequest), ctypes.POINTER(c_u64)]),
+    ("stocha_server_poll", c_i32, [c_void_p, c_u64, ctypes.POINTER(StochaResult)]),
+    ("stocha_server_wait", c_i32, [c_void_p, c_u64, c_dbl, ctypes.POINTER(StochaResult)]),
+    ("stocha_server_replay", c_i32, [c_void_p, ctypes.POINTER(StochaRequest), P_dbl, c_u64,
+                                     ctypes.POINTER(StochaResult)]),
+    ("stocha_server_stats", c_i32, [c_void_p, ctypes.POINTER(StochaServerCounters)]),
+    ("stocha_debug_arena", c_i32, [c_u64, ctypes.POINTER(ctypes.c_int64), c_u64, ctypes.POINTER(ctypes.c_int64)]),
     ("stocha_debug_zig_thresholds", c_i32, [P_u64]),
     ("stocha_debug_exp", c_i32, [c_void_p, P_dbl, P_dbl, c_u64]),
     ("stocha_measure_peak", c_i32, [c_void_p, c_i32, P_dbl]),

@@ -536,6 +536,7 @@ void stocha_ctx_destroy(stocha_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (DevBuf* b : {&c->out, &c->partials, &c->small, &c->aux, &c->starts})
     if (b->ptr) cudaFree(b->ptr);
+  if (c->lsmc_graphs) lsmc_graphs_release(c->lsmc_graphs);
   if (c->d_tabs) cudaFree(c->d_tabs);
   if (c->d_err) cudaFree(c->d_err);
   if (c->h_err) cudaFreeHost(c->h_err);

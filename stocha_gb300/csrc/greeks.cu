@@ -74,12 +74,15 @@ __device__ __forceinline__ void diffs(float S, float up, float dn, float dud, fl
   *g_out = g;
 }
 
-// Per-path contributions from the terminal values of the trajectories.
+// Per-path contributions from the terminal values of the trajectories (PO:
+// price only, the first two sums).
+template <bool PO>
 __device__ __forceinline__ void contribute(const GInst& I, float S, float S_sp, float S_sm, float S_tm, K32* acc) {
   const int call = I.payoff == kCall;
   const float p0 = pay(S, I.K, call);
   acc[0].add(p0);
   acc[1].add(p0 * p0);
+  if constexpr (PO) return;
   float d1, g;
   diffs(S, S * (1.0f + I.u), S * (1.0f - I.u), 2.0f * I.u, 0.0f, I.K, call, &d1, &g);
   acc[2].add(d1);
@@ -95,16 +98,18 @@ __device__ __forceinline__ void contribute(const GInst& I, float S, float S_sp, 
   acc[8].add(pay(sm, I.K, call));
 }
 
+template <bool PO>
 __device__ void path_gbm(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
                          K32* acc) {
   PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
   K32 w{0.0f, 0.0f};
   for (uint64_t k = 0; k < I.steps; ++k) w.add(normal_f32(g, c, zs, err));
   const float W = w.s - w.c;
+  constexpr int NT = PO ? 1 : 4;
   float S[4];
 #pragma unroll
-  for (int t = 0; t < 4; ++t) S[t] = I.s0 * expf(fmaf(I.diff[t], W, I.kdrift[t]));
-  contribute(I, S[0], S[1], S[2], S[3], acc);
+  for (int t = 0; t < NT; ++t) S[t] = I.s0 * expf(fmaf(I.diff[t], W, I.kdrift[t]));
+  contribute<PO>(I, S[0], S[PO ? 0 : 1], S[PO ? 0 : 2], S[PO ? 0 : 3], acc);
 }
 
 __device__ void merton_pass(const GInst& I, uint64_t p, uint64_t thr, const SamplerCtx& c, const ZigShared& zs,
@@ -120,30 +125,38 @@ __device__ void merton_pass(const GInst& I, uint64_t p, uint64_t thr, const Samp
   *J = jumps;
 }
 
+template <bool PO>
 __device__ void path_merton(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
                             K32* acc) {
   float W, J;
   merton_pass(I, p, I.jthr[0], c, zs, err, &W, &J);
   float S[4];
-#pragma unroll
-  for (int t = 0; t < 3; ++t) S[t] = I.s0 * expf(fmaf(I.diff[t], W, I.kdrift[t]) + J);
-  if (I.theta_pass) {
-    float W2, J2;
-    merton_pass(I, p, I.jthr[1], c, zs, err, &W2, &J2);
-    S[3] = I.s0 * expf(fmaf(I.diff[3], W2, I.kdrift[3]) + J2);
+  if constexpr (PO) {
+    S[0] = I.s0 * expf(fmaf(I.diff[0], W, I.kdrift[0]) + J);
+    contribute<true>(I, S[0], S[0], S[0], S[0], acc);
   } else {
-    S[3] = S[0];
+#pragma unroll
+    for (int t = 0; t < 3; ++t) S[t] = I.s0 * expf(fmaf(I.diff[t], W, I.kdrift[t]) + J);
+    if (I.theta_pass) {
+      float W2, J2;
+      merton_pass(I, p, I.jthr[1], c, zs, err, &W2, &J2);
+      S[3] = I.s0 * expf(fmaf(I.diff[3], W2, I.kdrift[3]) + J2);
+    } else {
+      S[3] = S[0];
+    }
+    contribute<false>(I, S[0], S[1], S[2], S[3], acc);
   }
-  contribute(I, S[0], S[1], S[2], S[3], acc);
 }
 
+template <bool PO>
 __device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
                             K32* acc) {
+  constexpr int NT = PO ? 1 : 4;
   PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
   float v[4];
   K32 lg[4];
 #pragma unroll
-  for (int t = 0; t < 4; ++t) {
+  for (int t = 0; t < NT; ++t) {
     v[t] = I.hv0[t];
     lg[t] = K32{0.0f, 0.0f};
   }
@@ -152,7 +165,7 @@ __device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, con
     const float dz = normal_f32(g, c, zs, err);
     const float dw2 = fmaf(I.hrho, dw1, I.hrho_comp * dz);
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
+    for (int t = 0; t < NT; ++t) {
       const float vp = fmaxf(v[t], 0.0f);
       const float sv = sqrtf(vp);
       v[t] += fmaf(I.hkdt[t], I.htheta - vp, I.hxsdt[t] * sv * dw2);
@@ -161,48 +174,82 @@ __device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, con
   }
   float S[4];
 #pragma unroll
-  for (int t = 0; t < 4; ++t) S[t] = I.s0 * expf(lg[t].s - lg[t].c);
-  contribute(I, S[0], S[1], S[2], S[3], acc);
+  for (int t = 0; t < NT; ++t) S[t] = I.s0 * expf(lg[t].s - lg[t].c);
+  contribute<PO>(I, S[0], S[PO ? 0 : 1], S[PO ? 0 : 2], S[PO ? 0 : 3], acc);
 }
 
+// Paths [lo, hi) of one instance, one per thread in turn, then the item's
+// block totals (compensated FP32 per thread and per warp, FP64 across warps).
+template <bool PO>
+__device__ __forceinline__ void run_item(const GInst& I, uint64_t lo, uint64_t hi, const SamplerCtx& c,
+                                         const ZigShared& zs, unsigned& err, double* out) {
+  constexpr int NA = PO ? 2 : kGreekAcc;
+  K32 acc[kGreekAcc];
+#pragma unroll
+  for (int j = 0; j < kGreekAcc; ++j) acc[j] = K32{0.0f, 0.0f};
+  for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    if (I.model == kGbm)
+      path_gbm<PO>(I, p, c, zs, err, acc);
+    else if (I.model == kHeston)
+      path_heston<PO>(I, p, c, zs, err, acc);
+    else
+      path_merton<PO>(I, p, c, zs, err, acc);
+  }
+  float s[NA], cc[NA];
+#pragma unroll
+  for (int j = 0; j < NA; ++j) {
+    s[j] = acc[j].s;
+    cc[j] = acc[j].c;
+  }
+  block_sum_kahan_store<NA>(s, cc, out);
+  if (PO && (int)threadIdx.x >= 2 && (int)threadIdx.x < kGreekAcc) out[threadIdx.x] = 0.0;
+}
+
+// Instance of an item: from the item map, or the last instance whose first
+// item is <= item (binary search over the ordered item_begin).
+__device__ __forceinline__ uint32_t inst_of_item(const GreeksLaunch& g, unsigned long long item) {
+  if (g.item_inst) return g.item_inst[item];
+  int lo = 0, hi = g.n_inst - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.inst[mid].item_begin <= item)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return (uint32_t)lo;
+}
+
+// A block serves items: the next from the queue counter (persistent grid) or
+// item blockIdx.x (direct: one block per item, so blocks retire after one
+// chunk and work on higher-priority streams gets SMs between them).
 __global__ void __launch_bounds__(256) k_greeks(const GreeksLaunch g) {
   __shared__ ZigShared zs;
   __shared__ unsigned long long item_s;
   zig_stage(zs, g.tabs, false);
   const SamplerCtx c{g.tabs, g.tabs->r32, g.tabs->r};
   unsigned err = 0;
-  for (;;) {
-    if (threadIdx.x == 0) item_s = atomicAdd(g.counter, 1ull);
-    __syncthreads();
-    const unsigned long long item = item_s;
-    __syncthreads();  // item_s is rewritten next round
+  for (unsigned long long round = 0;; ++round) {
+    unsigned long long item;
+    if (g.direct) {
+      if (round > 0) break;
+      item = blockIdx.x;
+    } else {
+      if (threadIdx.x == 0) item_s = atomicAdd(g.counter, 1ull);
+      __syncthreads();
+      item = item_s;
+      __syncthreads();  // item_s is rewritten next round
+    }
     if (item >= g.total_items) break;
-    const GInst& I = g.inst[g.item_inst[item]];
+    const GInst& I = g.inst[inst_of_item(g, item)];
     const uint64_t lo = (item - I.item_begin) * I.chunk;
     uint64_t hi = lo + I.chunk;
     if (hi > I.n_paths) hi = I.n_paths;
-    K32 acc[kGreekAcc];
-#pragma unroll
-    for (int j = 0; j < kGreekAcc; ++j) acc[j] = K32{0.0f, 0.0f};
-    for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
-      if (I.model == kGbm)
-        path_gbm(I, p, c, zs, err, acc);
-      else if (I.model == kHeston)
-        path_heston(I, p, c, zs, err, acc);
-      else
-        path_merton(I, p, c, zs, err, acc);
-    }
-#pragma unroll
-    for (int j = 0; j < kGreekAcc; j += 2) {
-      const double a = (double)(acc[j].s - acc[j].c);
-      const double b = j + 1 < kGreekAcc ? (double)(acc[j + 1].s - acc[j + 1].c) : 0.0;
-      double tmp[2];
-      block_sum2_store(a, b, tmp);  // thread 0 receives the block totals
-      if (threadIdx.x == 0) {
-        g.item_part[item * kGreekAcc + j] = tmp[0];
-        if (j + 1 < kGreekAcc) g.item_part[item * kGreekAcc + j + 1] = tmp[1];
-      }
-    }
+    double* out = g.item_part + item * kGreekAcc;
+    if (I.price_only)
+      run_item<true>(I, lo, hi, c, zs, err, out);
+    else
+      run_item<false>(I, lo, hi, c, zs, err, out);
   }
   if (err) atomicOr(g.err, err);
 }
@@ -227,8 +274,8 @@ void launch_greeks_batch(const GreeksLaunch& g, cudaStream_t st) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_greeks, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 2;
   uint64_t blocks = (uint64_t)sms * per_sm;
-  if (blocks > g.total_items) blocks = g.total_items ? g.total_items : 1;
-  cudaMemsetAsync(g.counter, 0, sizeof(unsigned long long), st);
+  if (blocks > g.total_items || g.direct) blocks = g.total_items ? g.total_items : 1;
+  if (!g.direct) cudaMemsetAsync(g.counter, 0, sizeof(unsigned long long), st);
   k_greeks<<<(unsigned)blocks, 256, 0, st>>>(g);
   k_greeks_finish<<<(g.n_inst + 127) / 128, 128, 0, st>>>(g);
 }

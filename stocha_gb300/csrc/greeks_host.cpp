@@ -180,9 +180,16 @@ int greeks_fp64(stocha_ctx* ctx, const stocha_model& base, int payoff, stocha_pa
   return STOCHA_OK;
 }
 
-// Fills one device instance of the FP32 batch kernel.
-void make_inst(const stocha_model& m, int payoff, double strike, double bump_size, uint64_t seed, GInst* I) {
+}  // namespace
+
+namespace stocha {
+
+// Fills one device instance of the FP32 batch kernel (price_only: the price
+// and its standard error only).
+void greeks_make_inst(const stocha_model& m, int payoff, double strike, double bump_size, uint64_t seed,
+                      bool price_only, GInst* I) {
   std::memset(I, 0, sizeof *I);
+  I->price_only = price_only ? 1 : 0;
   I->model = m.kind == STOCHA_MODEL_GBM ? kGbm : m.kind == STOCHA_MODEL_HESTON ? kHeston : kMerton;
   I->payoff = payoff;
   I->steps = m.steps;
@@ -258,6 +265,33 @@ void greeks_from_sums(const stocha_model& m, double bump_size, const double* S, 
   g[4] = disc * (std::exp(-hr * m.t) * (S[7] / n) - 2.0 * std::sinh(hr * m.t) * (S[8] / n)) / (2.0 * hr);
 }
 
+// The model of one batch instance (its r is the drift, greeks.rs:190-200).
+stocha_model greeks_model_of(const stocha_greeks_instance& x) {
+  stocha_model m;
+  std::memset(&m, 0, sizeof m);
+  m.kind = x.model;
+  m.scheme = x.scheme;
+  m.s0 = x.s0;
+  m.mu = x.r;
+  m.sigma = x.sigma;
+  m.t = x.t;
+  m.v0 = x.v0;
+  m.kappa = x.kappa;
+  m.theta = x.theta;
+  m.xi = x.xi;
+  m.rho = x.rho;
+  m.lambda_ = x.lambda_;
+  m.mu_j = x.mu_j;
+  m.sigma_j = x.sigma_j;
+  m.steps = x.steps;
+  m.n_paths = x.n_paths;
+  return m;
+}
+
+}  // namespace stocha
+
+namespace {
+
 int batch_fp32(stocha_ctx* ctx, const std::vector<stocha_model>& models, const std::vector<int>& payoffs,
                const std::vector<double>& strikes, const std::vector<double>& bumps,
                const std::vector<uint64_t>& seeds, std::vector<double>* sums) {
@@ -267,7 +301,7 @@ int batch_fp32(stocha_ctx* ctx, const std::vector<stocha_model>& models, const s
   std::vector<uint32_t> item_inst;
   uint64_t items = 0;
   for (uint64_t i = 0; i < n; ++i) {
-    make_inst(models[i], payoffs[i], strikes[i], bumps[i], seeds[i], &inst[i]);
+    greeks_make_inst(models[i], payoffs[i], strikes[i], bumps[i], seeds[i], false, &inst[i]);
     inst[i].chunk = chunk;
     inst[i].item_begin = items;
     const uint64_t k = (models[i].n_paths + chunk - 1) / chunk;
@@ -290,6 +324,7 @@ int batch_fp32(stocha_ctx* ctx, const std::vector<stocha_model>& models, const s
   g.inst_sums = (double*)(base + off_sums);
   g.n_inst = (int)n;
   g.tabs = ctx->d_tabs;
+  g.direct = 0;
   g.err = ctx->d_err;
   if ((rc = begin_call(ctx))) return rc;
   STOCHA_CUDA(cudaMemcpyAsync(base, inst.data(), n * sizeof(GInst), cudaMemcpyHostToDevice, ctx->stream));
@@ -301,28 +336,6 @@ int batch_fp32(stocha_ctx* ctx, const std::vector<stocha_model>& models, const s
   STOCHA_CUDA(cudaMemcpyAsync(sums->data(), g.inst_sums, n * kGreekAcc * 8, cudaMemcpyDeviceToHost, ctx->stream));
   // the host vectors above must outlive the asynchronous copies
   return finish_call(ctx);
-}
-
-stocha_model model_of(const stocha_greeks_instance& x) {
-  stocha_model m;
-  std::memset(&m, 0, sizeof m);
-  m.kind = x.model;
-  m.scheme = x.scheme;
-  m.s0 = x.s0;
-  m.mu = x.r;
-  m.sigma = x.sigma;
-  m.t = x.t;
-  m.v0 = x.v0;
-  m.kappa = x.kappa;
-  m.theta = x.theta;
-  m.xi = x.xi;
-  m.rho = x.rho;
-  m.lambda_ = x.lambda_;
-  m.mu_j = x.mu_j;
-  m.sigma_j = x.sigma_j;
-  m.steps = x.steps;
-  m.n_paths = x.n_paths;
-  return m;
 }
 
 }  // namespace
@@ -428,7 +441,7 @@ int stocha_greeks_batch(stocha_ctx* ctx, const stocha_greeks_instance* inst, uin
   std::vector<uint64_t> seeds, idx;
   const std::vector<int> all = {G_DELTA, G_GAMMA, G_VEGA, G_THETA, G_RHO};
   for (uint64_t i = 0; i < n; ++i) {
-    const stocha_model m = model_of(inst[i]);
+    const stocha_model m = greeks_model_of(inst[i]);
     const bool qe = m.kind == STOCHA_MODEL_HESTON && m.scheme == 1;
     if (precision == STOCHA_FP32 && !qe) {
       models.push_back(m);

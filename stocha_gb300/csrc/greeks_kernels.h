@@ -29,7 +29,7 @@ struct GInst {
   int model;   // kGbm / kHeston / kMerton
   int payoff;  // kCall / kPut
   int theta_pass;  // Merton: run the T-h scenario as a second pass
-  int pad;
+  int price_only;  // only sums 0 and 1 (the others are written as zero)
   uint64_t steps, n_paths, item_begin, chunk;
   uint64_t jthr[2];  // Merton jump thresholds at T and T-h
   float K, s0, u;    // s0 bump ratio u = h_s0 / s0
@@ -44,9 +44,10 @@ struct GInst {
 
 struct GreeksLaunch {
   const GInst* inst;           // device array
-  const uint32_t* item_inst;   // item -> instance
+  const uint32_t* item_inst;   // item -> instance (NULL: found from the instances' item_begin)
   uint64_t total_items;
-  unsigned long long* counter; // work-queue head (zeroed before launch)
+  unsigned long long* counter; // work-queue head (zeroed before launch; unused when direct)
+  int direct;                  // 1: one block per item, grid = total_items
   double* item_part;           // total_items * kGreekAcc
   double* inst_sums;           // n_inst * kGreekAcc
   int n_inst;

@@ -13,6 +13,8 @@ typedef unsigned __int128 u128;
 
 namespace stocha {
 
+struct LsmcGraphs;
+
 // Grow-only device buffer owned by a context.
 struct DevBuf {
   void* ptr = nullptr;
@@ -30,6 +32,7 @@ struct stocha_ctx {
   unsigned* h_err = nullptr;  // pinned
   double* h_small = nullptr;  // pinned, 4096 doubles for small results
   stocha::DevBuf out, partials, small, aux, starts;
+  stocha::LsmcGraphs* lsmc_graphs = nullptr;  // LSMC sweep graphs for this context's stream
   std::recursive_mutex mu;
 };
 
@@ -81,6 +84,18 @@ int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precis
 // Enqueues a launch writing the terminal price of every path (FP64).
 int terminal_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, double* out_dev);
 
+struct GInst;
+// One instance of the batched FP32 Greeks kernel (greeks_kernels.h) for a
+// call or put on GBM, Heston (Euler) or Merton; price_only: only the price
+// and its standard error.
+void greeks_make_inst(const stocha_model& m, int payoff, double strike, double bump_size, uint64_t seed,
+                      bool price_only, GInst* I);
+// Price, standard error and the five Greeks (delta gamma vega theta rho) of
+// one instance from its FP64 totals of the per-path sums.
+void greeks_from_sums(const stocha_model& m, double bump_size, const double* S, double* price, double* se,
+                      double* g);
+stocha_model greeks_model_of(const stocha_greeks_instance& x);
+
 // One LSMC American option (lsmc.rs:4-14) as a job over caller-owned device
 // buffers: the path array and the sweep scratch.
 struct LsmcJob {
@@ -93,9 +108,11 @@ int lsmc_validate(const LsmcJob& j);
 void lsmc_footprint(const LsmcJob& j, int sms, size_t* path_bytes, size_t* scratch_bytes);
 // Enqueues paths and sweep on st; *result_dev receives the device address of
 // {mean of discounted cash flows, sum of squared deviations}.  flat: path
-// launch with one path per thread (see PathLaunch::flat_grid).
+// launch with one path per thread (see PathLaunch::flat_grid).  graphs: the
+// stream's sweep graphs (lsmc_kernels.h), used by one job at a time.
 int lsmc_enqueue(const LsmcJob& j, int sms, void* paths, void* scratch, const ZigTables* tabs, unsigned* err,
-                 bool flat, cudaStream_t st, const double** result_dev);
+                 bool flat, cudaStream_t st, LsmcGraphs* graphs, const double** result_dev);
+void lsmc_graphs_release(LsmcGraphs* g);
 // Price and standard error from the two device results (lsmc.rs:100-114).
 void lsmc_estimate(const LsmcJob& j, const double* res2, double* price, double* std_err);
 

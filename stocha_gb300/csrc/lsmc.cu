@@ -401,7 +401,8 @@ __device__ __forceinline__ void finish_pass(const double* tot, bool solve, LsmcS
 constexpr int kMultiCluster = 8;
 
 template <typename T, int DEG>
-__global__ void __launch_bounds__(kThreads) k_lsmc(const __grid_constant__ LsmcLaunch a, uint64_t t, int mode) {
+__global__ void __launch_bounds__(kThreads) k_lsmc(const LsmcLaunch* __restrict__ ap, uint64_t t, int mode) {
+  const LsmcLaunch& a = *ap;
   cg::cluster_group cluster = cg::this_cluster();
   const unsigned rank = cluster.block_rank(), csz = cluster.num_blocks();
   const unsigned cid = blockIdx.x / csz, ncl = gridDim.x / csz;
@@ -558,8 +559,10 @@ cudaLaunchConfig_t cluster_config(unsigned grid, unsigned block, size_t smem, un
   return cfg;
 }
 
+// Multi-launch passes as one instantiated graph per shape (see LsmcGraphs).
 template <typename T, int DEG>
-void sweep_multi(const LsmcLaunch& a, cudaStream_t st) {
+cudaError_t sweep_multi(const LsmcLaunch& a0, cudaStream_t st, LsmcGraphs* G) {
+  if (!G) return cudaErrorInvalidValue;
   // one wave of whole clusters: no more than are resident at once (a.grid
   // sized the partial rows; fewer clusters use fewer of them)
   auto fn = k_lsmc<T, DEG>;
@@ -572,15 +575,53 @@ void sweep_multi(const LsmcLaunch& a, cudaStream_t st) {
     cudaGetLastError();
     max_clusters = v;
   }
-  uint64_t want = ((uint64_t)a.grid + kMultiCluster - 1) / kMultiCluster;
+  uint64_t want = ((uint64_t)a0.grid + kMultiCluster - 1) / kMultiCluster;
   if (want > (uint64_t)max_clusters) want = max_clusters;
   if (want < 1) want = 1;
   const unsigned g = (unsigned)want * kMultiCluster;
-  cudaLaunchConfig_t cfg = cluster_config(g, kThreads, 0, kMultiCluster, st, attr);
-  cudaLaunchKernelEx(&cfg, fn, a, (uint64_t)a.steps, (int)kInit);
-  for (uint64_t t = a.steps - 1; t >= 1; --t) cudaLaunchKernelEx(&cfg, fn, a, t, (int)kStep);
-  cudaLaunchKernelEx(&cfg, fn, a, (uint64_t)0, (int)kFinal);
-  cudaLaunchKernelEx(&cfg, fn, a, (uint64_t)0, (int)kVar);
+
+  LsmcLaunch a = a0;
+  a.counter = (unsigned*)(G->d_params + 1);
+  *G->h_params = a;  // read by the graph's first node when it runs
+  const int f32 = sizeof(T) == 4;
+  for (int i = 0; i < G->n_cache; ++i) {
+    const LsmcGraphs::Entry& e = G->cache[i];
+    if (e.steps == a.steps && e.deg == DEG && e.f32 == f32 && e.grid == (int)g) return cudaGraphLaunch(e.exec, st);
+  }
+  // params upload, counter reset, steps + 2 passes
+  auto enqueue = [&](cudaStream_t s) {
+    cudaMemcpyAsync(G->d_params, G->h_params, sizeof(LsmcLaunch), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(a.counter, 0, sizeof(unsigned), s);
+    cudaLaunchConfig_t cfg = cluster_config(g, kThreads, 0, kMultiCluster, s, attr);
+    const LsmcLaunch* ap = G->d_params;
+    cudaLaunchKernelEx(&cfg, fn, ap, (uint64_t)a.steps, (int)kInit);
+    for (uint64_t t = a.steps - 1; t >= 1; --t) cudaLaunchKernelEx(&cfg, fn, ap, t, (int)kStep);
+    cudaLaunchKernelEx(&cfg, fn, ap, (uint64_t)0, (int)kFinal);
+    cudaLaunchKernelEx(&cfg, fn, ap, (uint64_t)0, (int)kVar);
+  };
+  if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+    cudaGetLastError();  // a stream that cannot be captured (the legacy default stream): plain launches
+    enqueue(st);
+    return cudaGetLastError();
+  }
+  enqueue(st);
+  cudaGraph_t graph = nullptr;
+  cudaError_t err = cudaStreamEndCapture(st, &graph);
+  if (err) return err;
+  cudaGraphExec_t exec = nullptr;
+  err = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (err) return err;
+  int slot;
+  if (G->n_cache < 8) {
+    slot = G->n_cache++;
+  } else {  // replace the oldest (an exec still running is freed when it completes)
+    slot = G->next;
+    G->next = (G->next + 1) % 8;
+    cudaGraphExecDestroy(G->cache[slot].exec);
+  }
+  G->cache[slot] = LsmcGraphs::Entry{a.steps, DEG, f32, (int)g, exec};
+  return cudaGraphLaunch(exec, st);
 }
 
 template <typename T, int DEG>
@@ -597,20 +638,17 @@ cudaError_t sweep_cluster(const LsmcLaunch& a, cudaStream_t st) {
 }
 
 template <typename T, int DEG>
-void sweep(const LsmcLaunch& a, cudaStream_t st) {
-  if (a.cluster > 0)
-    sweep_cluster<T, DEG>(a, st);
-  else
-    sweep_multi<T, DEG>(a, st);
+cudaError_t sweep(const LsmcLaunch& a, cudaStream_t st, LsmcGraphs* G) {
+  return a.cluster > 0 ? sweep_cluster<T, DEG>(a, st) : sweep_multi<T, DEG>(a, st, G);
 }
 
 template <typename T>
-void sweep_deg(const LsmcLaunch& a, cudaStream_t st) {
+cudaError_t sweep_deg(const LsmcLaunch& a, cudaStream_t st, LsmcGraphs* G) {
   switch (a.deg) {
-    case 1: sweep<T, 1>(a, st); break;
-    case 2: sweep<T, 2>(a, st); break;
-    case 3: sweep<T, 3>(a, st); break;
-    default: sweep<T, 4>(a, st); break;
+    case 1: return sweep<T, 1>(a, st, G);
+    case 2: return sweep<T, 2>(a, st, G);
+    case 3: return sweep<T, 3>(a, st, G);
+    default: return sweep<T, 4>(a, st, G);
   }
 }
 
@@ -668,12 +706,30 @@ void lsmc_bind_scratch(LsmcLaunch* a, void* scratch) {
   a->result = (double*)p;
 }
 
-void lsmc_sweep(const LsmcLaunch& a, cudaStream_t st) {
-  cudaMemsetAsync(a.counter, 0, sizeof(unsigned), st);
-  if (a.spot_f32)
-    sweep_deg<float>(a, st);
-  else
-    sweep_deg<double>(a, st);
+cudaError_t lsmc_graphs_create(LsmcGraphs** out) {
+  LsmcGraphs* g = new LsmcGraphs();
+  cudaError_t e;
+  if ((e = cudaMalloc((void**)&g->d_params, sizeof(LsmcLaunch) + 256)) ||
+      (e = cudaMallocHost((void**)&g->h_params, sizeof(LsmcLaunch)))) {
+    lsmc_graphs_destroy(g);
+    *out = nullptr;
+    return e;
+  }
+  *out = g;
+  return cudaSuccess;
+}
+
+void lsmc_graphs_destroy(LsmcGraphs* g) {
+  if (!g) return;
+  for (int i = 0; i < g->n_cache; ++i)
+    if (g->cache[i].exec) cudaGraphExecDestroy(g->cache[i].exec);
+  if (g->d_params) cudaFree(g->d_params);
+  if (g->h_params) cudaFreeHost(g->h_params);
+  delete g;
+}
+
+cudaError_t lsmc_sweep(const LsmcLaunch& a, cudaStream_t st, LsmcGraphs* graphs) {
+  return a.spot_f32 ? sweep_deg<float>(a, st, graphs) : sweep_deg<double>(a, st, graphs);
 }
 
 }  // namespace stocha

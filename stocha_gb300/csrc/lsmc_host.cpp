@@ -28,8 +28,10 @@ void lsmc_footprint(const LsmcJob& j, int sms, size_t* path_bytes, size_t* scrat
   *scratch_bytes = lsmc_scratch_bytes(j.n_paths, j.steps, lsmc_grid(j.n_paths, sms));
 }
 
+void lsmc_graphs_release(LsmcGraphs* g) { lsmc_graphs_destroy(g); }
+
 int lsmc_enqueue(const LsmcJob& j, int sms, void* paths, void* scratch, const ZigTables* tabs, unsigned* err,
-                 bool flat, cudaStream_t st, const double** result_dev) {
+                 bool flat, cudaStream_t st, LsmcGraphs* graphs, const double** result_dev) {
   // GBM paths under the risk-neutral drift (lsmc.rs:29-39)
   stocha_model m;
   std::memset(&m, 0, sizeof m);
@@ -76,7 +78,7 @@ int lsmc_enqueue(const LsmcJob& j, int sms, void* paths, void* scratch, const Zi
 
   const int g = f32 ? launch_paths_f32(L, st) : launch_paths_f64(L, st);
   if (g < 0) return cuda_error(cudaGetLastError(), "LSMC path launch");
-  lsmc_sweep(a, st);
+  STOCHA_CUDA(lsmc_sweep(a, st, graphs));
   STOCHA_CUDA(cudaGetLastError());
   *result_dev = a.result;
   return STOCHA_OK;
@@ -106,9 +108,11 @@ int lsmc_run(stocha_ctx* ctx, const LsmcJob& j, double* price, double* std_err) 
   lsmc_footprint(j, sms, &path_bytes, &scratch_bytes);
   if ((rc = ensure_buf(ctx, ctx->out, path_bytes))) return rc;
   if ((rc = ensure_buf(ctx, ctx->aux, scratch_bytes))) return rc;
+  if (!ctx->lsmc_graphs) STOCHA_CUDA(lsmc_graphs_create(&ctx->lsmc_graphs));
   if ((rc = begin_call(ctx))) return rc;
   const double* res = nullptr;
-  if ((rc = lsmc_enqueue(j, sms, ctx->out.ptr, ctx->aux.ptr, ctx->d_tabs, ctx->d_err, false, ctx->stream, &res)))
+  if ((rc = lsmc_enqueue(j, sms, ctx->out.ptr, ctx->aux.ptr, ctx->d_tabs, ctx->d_err, false, ctx->stream,
+                         ctx->lsmc_graphs, &res)))
     return rc;
   STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, res, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if ((rc = finish_call(ctx))) return rc;

@@ -45,8 +45,29 @@ int lsmc_cluster_size(uint64_t n, uint64_t steps, int f32);
 // binding of a LsmcLaunch's scratch pointers into it (256-byte aligned base).
 size_t lsmc_scratch_bytes(uint64_t n, uint64_t steps, int grid);
 void lsmc_bind_scratch(LsmcLaunch* a, void* scratch);
+// Instantiated CUDA graphs of the multi-launch sweep for one stream.  The
+// multi-launch kernels read their LsmcLaunch from device memory (params), so
+// one graph per shape (steps, degree, precision, grid) serves every job: a
+// graph launch copies the job's LsmcLaunch from the pinned staging, zeroes
+// the block counter and runs the steps + 2 passes.  The staging is read when
+// the graph runs: one job at a time per LsmcGraphs (a stream's jobs are in
+// order, and the host writes the staging only after the previous job ended).
+struct LsmcGraphs {
+  LsmcLaunch* d_params = nullptr;  // device: the launch description, then the block counter
+  LsmcLaunch* h_params = nullptr;  // pinned host staging
+  struct Entry {
+    uint64_t steps;
+    int deg, f32, grid;
+    cudaGraphExec_t exec;
+  };
+  Entry cache[8];
+  int n_cache = 0, next = 0;
+};
+cudaError_t lsmc_graphs_create(LsmcGraphs** out);
+void lsmc_graphs_destroy(LsmcGraphs* g);
+
 // Enqueues the whole sweep on `st` with no host round trip: one cluster
-// launch, or a zeroing of the block counter and steps + 2 launches.
-void lsmc_sweep(const LsmcLaunch& a, cudaStream_t st);
+// launch, or one graph launch of the multi-launch passes (graphs required).
+cudaError_t lsmc_sweep(const LsmcLaunch& a, cudaStream_t st, LsmcGraphs* graphs);
 
 }  // namespace stocha

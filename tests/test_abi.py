@@ -169,3 +169,54 @@ def test_lsmc_validation_messages(stocha):
         with pytest.raises(ValueError) as ei:
             fn()
         assert str(ei.value) == msg
+
+
+def test_serving_arena_host_logic(stocha):
+    """The serving loop's device-memory arena (first fit, 256-byte blocks,
+    coalescing on release) on host-only scripts: no two live blocks overlap,
+    every block is aligned and inside the budget, a full release coalesces
+    back to one free block, and a request larger than the largest free block
+    is refused."""
+    import ctypes
+
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(5)
+    cap = 1 << 20
+    for trial in range(20):
+        ops, live = [], []
+        for i in range(400):
+            if live and rng.random() < 0.45:
+                k = live.pop(int(rng.integers(len(live))))
+                ops.append(-k)
+            else:
+                ops.append(int(rng.integers(1, 60_000)))
+                live.append(i)
+        # then release everything still live
+        ops += [-k for k in live]
+        n = len(ops)
+        a = np.array(ops, np.int64)
+        res = np.zeros(n + 4, np.int64)
+        P = ctypes.POINTER(ctypes.c_int64)
+        assert lib.stocha_debug_arena(cap, a.ctypes.data_as(P), n, res.ctypes.data_as(P)) == 0
+        blocks = {}
+        for i, op in enumerate(ops):
+            if op > 0 and res[i] >= 0:
+                size = (op + 255) // 256 * 256
+                off = int(res[i])
+                assert off % 256 == 0 and off + size <= cap
+                for o2, s2 in blocks.values():
+                    assert off + size <= o2 or o2 + s2 <= off, "overlap"
+                blocks[i] = (off, size)
+            elif op <= 0:
+                blocks.pop(-op, None)
+        used, peak, largest, nfree = res[n:]
+        assert used == 0 and peak <= cap and largest == cap and nfree == 1
+    # refusal: two halves, free the first, a 3/4 request does not fit
+    ops = np.array([cap // 2, cap // 2, -0, 3 * cap // 4], np.int64)
+    ops[2] = 0  # releases allocation 0
+    res = np.zeros(8, np.int64)
+    P = ctypes.POINTER(ctypes.c_int64)
+    lib.stocha_debug_arena(cap, ops.ctypes.data_as(P), 4, res.ctypes.data_as(P))
+    assert res[0] == 0 and res[1] == cap // 2 and res[3] == -1
