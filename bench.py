@@ -370,6 +370,24 @@ def host_cores():
         return os.cpu_count() or 1
 
 
+def rank_max(x: float, world: int, device: str = "cuda") -> float:
+    """The maximum of x over the ranks of the process group (x itself for one
+    rank): the job's time is its slowest rank's."""
+    if world <= 1:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Seed of rank `rank`'s replica: every rank prices its own independent
+    paths of the same workload (weak scaling; no data-path collective)."""
+    return SEED + rank
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -415,7 +433,7 @@ def run_ours(args, rank, world):
     _lib.check(lib.stocha_ctx_create(dev, ctypes.byref(ctx)))
     stream = torch.cuda.Stream()
     _lib.check(lib.stocha_ctx_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)))
-    seed = SEED + rank  # weak scaling: each rank prices its own independent 1e6 paths per model
+    seed = replica_seed(rank)  # weak scaling: each rank prices its own independent 1e6 paths per model
 
     models = [(name, stocha.model_struct(name, p, STEPS, N_PATHS)) for name, p in WORKLOAD]
     sums = torch.zeros(64, dtype=torch.float64, device="cuda")
@@ -430,11 +448,7 @@ def run_ours(args, rank, world):
             torch.distributed.barrier()
 
     def max_over_ranks(x):
-        if world > 1:
-            t = torch.tensor([x], dtype=torch.float64, device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            return float(t.item())
-        return x
+        return rank_max(x, world, "cuda")
 
     path_steps = 3 * N_PATHS * STEPS
     # ---- headline: FP32 fused, device resident
