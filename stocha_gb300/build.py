@@ -34,7 +34,8 @@ CUDA_UNITS = {
     "peaks.cu": [],
     "noalloc.cu": [],
 }
-HOST_UNITS = ["api.cpp", "rng_host.cpp", "lsmc_host.cpp", "greeks_host.cpp", "batch_host.cpp", "serve.cpp"]
+HOST_UNITS = ["api.cpp", "rng_host.cpp", "lsmc_host.cpp", "greeks_host.cpp", "batch_host.cpp", "serve.cpp",
+              "hostcopy.cpp"]
 
 
 def _cuda_home() -> str:

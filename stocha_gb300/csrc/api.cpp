@@ -463,7 +463,7 @@ static int paths_to_host(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, 
   if ((rc = ensure_buf(ctx, ctx->out, bytes))) return rc;
   if ((rc = begin_call(ctx))) return rc;
   if ((rc = paths_to_device(ctx, m, seed, STOCHA_FP64, ctx->out.ptr))) return rc;
-  STOCHA_CUDA(cudaMemcpyAsync(out, ctx->out.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if ((rc = copy_to_host_populated(ctx->stream, out, ctx->out.ptr, bytes))) return rc;
   return finish_call(ctx);
 }
 

@@ -81,6 +81,11 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
 // of the payoff per asset.  aux4: payoff parameters (pathwise estimators).
 int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precision, int payoff, double strike,
                  const double* aux4, bool check, double* sums_dev, int* nvals);
+// Enqueues the copy of a large device result into fresh pageable host memory
+// after the work already on st: the destination's pages are populated by host
+// threads in the meantime and the copy goes out in chunks as they are ready
+// (hostcopy.cpp).  Returns after the last chunk is enqueued.
+int copy_to_host_populated(cudaStream_t st, void* dst, const void* src, size_t bytes);
 // Enqueues a launch writing the terminal price of every path (FP64).
 int terminal_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, double* out_dev);
 

@@ -59,7 +59,7 @@ int fill_raw(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, void* out) {
   if ((rc = begin_call(ctx))) return rc;
   launch_rng_raw(ss, stride, threads, n, kind, ctx->out.ptr, ctx->stream);
   STOCHA_CUDA(cudaGetLastError());
-  STOCHA_CUDA(cudaMemcpyAsync(out, ctx->out.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  if ((rc = copy_to_host_populated(ctx->stream, out, ctx->out.ptr, bytes))) return rc;
   if ((rc = finish_call(ctx))) return rc;
   u128 s = rng_state(r);
   pcg_advance(&s, rng_inc(r), n);
@@ -112,7 +112,7 @@ int fill_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, double loc
     launch_rng_emit(ss, ctx->d_tabs, nchunks, C, entry, cnt, offset, n, kind, loc, scale, (double*)ctx->out.ptr,
                     final_pos, ctx->d_err, ctx->stream);
     STOCHA_CUDA(cudaGetLastError());
-    STOCHA_CUDA(cudaMemcpyAsync(out, ctx->out.ptr, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = copy_to_host_populated(ctx->stream, out, ctx->out.ptr, n * 8))) return rc;
     STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, final_pos, 8, cudaMemcpyDeviceToHost, ctx->stream));
     if ((rc = finish_call(ctx))) return rc;
     uint64_t fp;
