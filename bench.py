@@ -9,6 +9,9 @@ One "step" = one pass of all three models.  Path-steps per step = 3 * 2.52e8
           timed with CUDA events on the launching stream.
   e2e     the same through the public API stocha_gb300.price_european
           (host call: parameters in, (price, se) out, copies included).
+  autotune  the fused FP32 kernels' launch shapes (threads per block, paths
+          per thread in lockstep, grid waves), timed on this workload before
+          the timed region; the chosen shape and its gain over the default.
   fp64_plain   FP64 materialised paths (reference arithmetic) of the same
           workload into device memory (10.1 GB per step) and, end to end,
           through stocha_gb300.multi_gbm/heston/merton_jump_diffusion into
@@ -436,6 +439,11 @@ def run_ours(args, rank, world):
     seed = replica_seed(rank)  # weak scaling: each rank prices its own independent 1e6 paths per model
 
     models = [(name, stocha.model_struct(name, p, STEPS, N_PATHS)) for name, p in WORKLOAD]
+    # launch shapes of the fused FP32 kernels, tuned on this workload before any timing
+    tuning = {}
+    if not args.no_tune:
+        for name, p in WORKLOAD:
+            tuning[name] = stocha.autotune(name, p, steps=STEPS, n_paths=N_PATHS, reps=3)
     sums = torch.zeros(64, dtype=torch.float64, device="cuda")
 
     def fused_step():
@@ -571,6 +579,7 @@ def run_ours(args, rank, world):
                          "unit": "Gdraws/s", "frac": achieved / peak_draws.value, "traffic": None,
                          "kernel_ms": per_model, "peak_source": "measured live (stocha_measure_peak kind 3)"},
             "fp64_plain": fp64,
+            "autotune": tuning,
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
         }
@@ -592,6 +601,7 @@ def main():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-extras", action="store_true", help="only the headline workload")
     ap.add_argument("--paths", type=int, default=N_PATHS, help="paths per model (profiling cases)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default launch shapes (no autotune)")
     args = ap.parse_args()
     globals()["N_PATHS"] = args.paths
     rank = int(os.environ.get("RANK", "0"))

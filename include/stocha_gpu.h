@@ -243,6 +243,28 @@ int stocha_rng_from_state(const char* json, stocha_rng* out);
  * check the device generator against the reference bit for bit). */
 int stocha_rng_raw_u64(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, uint64_t* out);
 
+/* ------------------------------------------------------------- autotuner
+ * No counterpart in the reference.  The fused FP32 pricing kernels have a
+ * launch shape per model kind: the kernel form (variant 0: one path per
+ * thread at a time; variant 1: ilp paths per thread in lockstep, 1 or 2),
+ * threads per block (64/128/256) and grid waves (1 or 2 times the resident
+ * blocks): 18 shapes.  stocha_autotune times every shape on the given model
+ * and size (reps launches each, CUDA events on the context's stream) and
+ * installs the fastest for that model kind; the table is process-wide.
+ * Draws and per-path values do not depend on the shape; the grouping of the
+ * FP32 payoff partial sums does (their last bits). */
+typedef struct stocha_tune_result {
+  int32_t model, n_assets; /* STOCHA_MODEL_*; n_assets for multi-GBM (1..4) */
+  int32_t block, ilp, waves, variant;
+  int32_t candidates;      /* shapes timed */
+  int32_t pad;
+  double ms_best, ms_default; /* per launch: the chosen shape, and variant 0 / 256 / 1 wave */
+} stocha_tune_result;
+
+int stocha_autotune(stocha_ctx* ctx, const stocha_model* m, int32_t reps, stocha_tune_result* out);
+int stocha_tune_get(int32_t model, int32_t n_assets, stocha_tune_result* out);
+int stocha_tune_set(int32_t model, int32_t n_assets, int32_t block, int32_t ilp, int32_t waves, int32_t variant);
+
 /* -------------------------------------------------------------- serving
  * No counterpart in the reference (its API is one blocking call per
  * pricing).  A server owns one device-memory budget, a set of CUDA streams

@@ -38,6 +38,9 @@ __all__ = [
     "greeks_batch",
     "price_european",
     "model_struct",
+    "autotune",
+    "tune_get",
+    "tune_set",
     "Server",
     "__version__",
 ]
@@ -229,3 +232,35 @@ def price_european(model: str, params: dict, strike: float, payoff: str = "call"
                                         float(rate), _lib.dptr(out)))
     res = [(float(out[2 * a]), float(out[2 * a + 1])) for a in range(na)]
     return res if model == "multi_gbm" else res[0]
+
+
+def _tune_dict(r) -> dict:
+    return {"variant": r.variant, "block": r.block, "ilp": r.ilp, "waves": r.waves, "candidates": r.candidates,
+            "ms_best": r.ms_best, "ms_default": r.ms_default}
+
+
+def autotune(model: str, params: dict, steps: int = 252, n_paths: int = 1_000_000, reps: int = 3) -> dict:
+    """Times every launch shape of the fused FP32 pricing kernel of ``model``
+    (kernel form: one path per thread at a time, or 1 or 2 paths per thread
+    in lockstep; threads per block 64/128/256; 1 or 2 waves of resident
+    blocks) on this size and installs the fastest for the model kind
+    (process-wide).  Returns the chosen shape with its time and the default
+    shape's time (ms per launch)."""
+    m = model_struct(model, params, steps, n_paths)
+    r = _lib.StochaTuneResult()
+    _lib.check(_lib.load().stocha_autotune(None, ctypes.byref(m), int(reps), ctypes.byref(r)))
+    return _tune_dict(r)
+
+
+def tune_get(model: str, n_assets: int = 0) -> dict:
+    """The installed launch shape of ``model``'s fused FP32 kernel."""
+    r = _lib.StochaTuneResult()
+    _lib.check(_lib.load().stocha_tune_get(_KINDS[model], int(n_assets), ctypes.byref(r)))
+    return _tune_dict(r)
+
+
+def tune_set(model: str, block: int, ilp: int, waves: int, variant: int = 1, n_assets: int = 0) -> None:
+    """Installs a launch shape (e.g. one saved from an earlier autotune)."""
+    _lib.check(_lib.load().stocha_tune_set(_KINDS[model], int(n_assets), int(block), int(ilp), int(waves),
+                                           int(variant)))
+

@@ -76,6 +76,11 @@ class StochaServerCounters(ctypes.Structure):
         [("lanes", c_i32), ("high_lanes", c_i32)]
 
 
+class StochaTuneResult(ctypes.Structure):
+    _fields_ = [(k, c_i32) for k in ("model", "n_assets", "block", "ilp", "waves", "variant", "candidates", "pad")] + \
+        [("ms_best", c_dbl), ("ms_default", c_dbl)]
+
+
 PAYOFF_FN = ctypes.CFUNCTYPE(c_i32, c_void_p, P_dbl, c_u64, P_dbl, ctypes.POINTER(c_u64))
 P_charp = ctypes.POINTER(ctypes.c_char_p)
 
@@ -118,6 +123,9 @@ SIGNATURES = [
     ("stocha_greeks_pathwise", c_i32, [c_void_p] + [c_dbl] * 5 + [c_i32, c_u64, c_u64, P_charp, c_u64, c_u64, P_dbl]),
     ("stocha_greeks_batch", c_i32, [c_void_p, ctypes.POINTER(StochaGreeksInstance), c_u64, c_i32, P_dbl]),
     ("stocha_price_noalloc", c_i32, [ctypes.POINTER(StochaModel), c_u64, c_i32, c_i32, c_dbl, c_void_p, c_void_p]),
+    ("stocha_autotune", c_i32, [c_void_p, ctypes.POINTER(StochaModel), c_i32, ctypes.POINTER(StochaTuneResult)]),
+    ("stocha_tune_get", c_i32, [c_i32, c_i32, ctypes.POINTER(StochaTuneResult)]),
+    ("stocha_tune_set", c_i32, [c_i32, c_i32, c_i32, c_i32, c_i32, c_i32]),
     ("stocha_server_create", c_i32, [c_i32, c_u64, c_i32, ctypes.POINTER(c_void_p)]),
     ("stocha_server_destroy", c_i32, [c_void_p]),
     ("stocha_server_submit", c_i32, [c_void_p, ctypes.POINTER(StochaRequest), ctypes.POINTER(c_u64)]),

@@ -581,6 +581,109 @@ int stocha_measure_peak(stocha_ctx* ctx, int32_t kind, double* ops_per_s) {
   return STOCHA_OK;
 }
 
+static int tune_slot_of(int32_t model, int32_t n_assets) {
+  const int kind = model == STOCHA_MODEL_GBM ? kGbm : model == STOCHA_MODEL_HESTON ? kHeston
+                   : model == STOCHA_MODEL_MERTON ? kMerton : model == STOCHA_MODEL_MULTI_GBM ? kMultiGbm : -1;
+  return kind < 0 ? -1 : tune_slot(kind, n_assets);
+}
+
+int stocha_tune_get(int32_t model, int32_t n_assets, stocha_tune_result* out) {
+  const int slot = tune_slot_of(model, n_assets);
+  if (slot < 0 || !out) return set_error(STOCHA_ERR_VALUE, "no fused FP32 kernel for this model");
+  const FusedTune t = get_fused_tune(slot);
+  std::memset(out, 0, sizeof *out);
+  out->model = model;
+  out->n_assets = n_assets;
+  out->block = t.block;
+  out->ilp = t.ilp;
+  out->waves = t.waves;
+  out->variant = t.variant;
+  return STOCHA_OK;
+}
+
+int stocha_tune_set(int32_t model, int32_t n_assets, int32_t block, int32_t ilp, int32_t waves, int32_t variant) {
+  const int slot = tune_slot_of(model, n_assets);
+  if (slot < 0) return set_error(STOCHA_ERR_VALUE, "no fused FP32 kernel for this model");
+  if (set_fused_tune(slot, FusedTune{block, ilp, waves, variant}))
+    return set_error(STOCHA_ERR_VALUE,
+                     "block must be 64, 128 or 256; waves 1 or 2; variant 0 (ilp 1) or 1 (ilp 1 or 2)");
+  return STOCHA_OK;
+}
+
+int stocha_autotune(stocha_ctx* ctx, const stocha_model* m, int32_t reps, stocha_tune_result* out) {
+  if (!m || !out) return set_error(STOCHA_ERR_VALUE, "model and out must not be NULL");
+  const int slot = tune_slot_of(m->kind, m->n_assets);
+  if (slot < 0 || (m->kind == STOCHA_MODEL_HESTON && m->scheme != 0))
+    return set_error(STOCHA_ERR_VALUE, "no fused FP32 kernel for this model");
+  {
+    PathLaunch probe;
+    uint64_t row_len = 0;
+    u128 block = 0;
+    int rc = prepare_model(m, &probe, &row_len, &block);
+    if (rc) return rc;
+  }
+  if (reps < 1) reps = 1;
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if ((rc = ensure_buf(ctx, ctx->small, 64 * sizeof(double)))) return rc;
+  double* sums = (double*)ctx->small.ptr;
+  cudaEvent_t e0, e1;
+  STOCHA_CUDA(cudaEventCreate(&e0));
+  STOCHA_CUDA(cudaEventCreate(&e1));
+  const FusedTune before = get_fused_tune(slot);
+  auto time_cfg = [&](FusedTune t, double* ms) -> int {
+    set_fused_tune(slot, t);
+    int nv = 0, r;
+    if ((r = begin_call(ctx))) return r;
+    if ((r = price_launch(ctx, m, 1, STOCHA_FP32, kCall, m->s0, nullptr, true, sums, &nv))) return r;  // warm-up
+    STOCHA_CUDA(cudaEventRecord(e0, ctx->stream));
+    for (int i = 0; i < reps; ++i)
+      if ((r = price_launch(ctx, m, 1 + i, STOCHA_FP32, kCall, m->s0, nullptr, true, sums, &nv))) return r;
+    STOCHA_CUDA(cudaEventRecord(e1, ctx->stream));
+    if ((r = finish_call(ctx))) return r;
+    float f = 0.0f;
+    STOCHA_CUDA(cudaEventElapsedTime(&f, e0, e1));
+    *ms = (double)f / reps;
+    return STOCHA_OK;
+  };
+  FusedTune best = before;
+  double best_ms = 1e300, default_ms = 0.0;
+  int n = 0;
+  rc = STOCHA_OK;
+  const int forms[3][2] = {{0, 1}, {1, 1}, {1, 2}};  // (variant, ilp)
+  for (int b : {64, 128, 256})
+    for (const auto& fm : forms)
+      for (int waves : {1, 2}) {
+        if (rc) break;
+        double ms = 0.0;
+        const FusedTune t{b, fm[1], waves, fm[0]};
+        if ((rc = time_cfg(t, &ms))) break;
+        ++n;
+        if (b == 256 && fm[0] == 0 && waves == 1) default_ms = ms;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = t;
+        }
+      }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  set_fused_tune(slot, rc ? before : best);
+  if (rc) return rc;
+  std::memset(out, 0, sizeof *out);
+  out->model = m->kind;
+  out->n_assets = m->n_assets;
+  out->block = best.block;
+  out->ilp = best.ilp;
+  out->waves = best.waves;
+  out->variant = best.variant;
+  out->candidates = n;
+  out->ms_best = best_ms;
+  out->ms_default = default_ms;
+  return STOCHA_OK;
+}
+
 int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n) {
   int rc = resolve_ctx(&ctx);
   if (rc) return rc;

@@ -75,6 +75,19 @@ struct PathLaunch {
   F32K f32;
 };
 
+// Launch shape of the fused FP32 pricing kernels, per model kind (tuning
+// slot: 0 gbm, 1 heston, 2 merton, 3..6 multi-GBM with 1..4 assets).
+struct FusedTune {
+  int block;    // threads per block: 64, 128 or 256
+  int ilp;      // paths per thread in lockstep: 1 or 2 (lockstep form)
+  int waves;    // grid = waves * resident blocks (1 or 2)
+  int variant;  // 0: per-path loop kernel (ilp 1); 1: lockstep kernel
+};
+constexpr int kTuneSlots = 7;
+int tune_slot(int model, int na);  // -1: no fused FP32 kernel for this model
+FusedTune get_fused_tune(int slot);
+int set_fused_tune(int slot, FusedTune t);  // 0, or -1 for an invalid slot or shape
+
 // Rounds the FP32 constants of L (after the model constants are set).
 void fill_f32_constants(PathLaunch* L);
 

@@ -210,6 +210,240 @@ __global__ void __launch_bounds__(256) k_merton_f32(const __grid_constant__ Path
   if (err) atomicOr(a.err, err);
 }
 
+// ------------------------------------------------------------ fused -------
+// Fused pricing (payoff sums only) with ILP paths per thread in lockstep: the
+// paths' generator steps are independent instruction chains (normal2_f32), so
+// the issue slots fill from two streams per warp.  The block size, ILP and
+// grid waves are chosen per model by the autotuner (set_fused_tune); every
+// choice draws the same values for every path, only the grouping of the
+// FP32 payoff partial sums (hence their last bits) changes with it.
+
+template <int ILP>
+__device__ __forceinline__ void normals(PcgGen* s, float* z, const SamplerCtx& c, const ZigShared& zs, unsigned& err) {
+  if constexpr (ILP == 1)
+    z[0] = normal_f32(s[0], c, zs, err);
+  else
+    normal2_f32(s[0], s[1], c, zs, err, z[0], z[1]);
+}
+
+// Rows l0 + j * nthreads (j < ILP) of one lockstep group; a row past the end
+// runs on a copy of the first row's stream and contributes nothing.
+template <int ILP>
+__device__ __forceinline__ void group_rows(const PathLaunch& a, uint64_t l0, uint64_t nthreads, bool* ok, bool* neg,
+                                           PcgGen* s) {
+#pragma unroll
+  for (int j = 0; j < ILP; ++j) {
+    const uint64_t lrow = l0 + (uint64_t)j * nthreads;
+    ok[j] = lrow < a.rows;
+    const uint64_t row = a.row_begin + (ok[j] ? lrow : l0);
+    neg[j] = row >= a.base_paths;
+    s[j] = PcgGen{pcg_path_state(a.ss, neg[j] ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
+  }
+}
+
+template <int NV>
+__device__ __forceinline__ void store_partials(const PathLaunch& a, const Kahan* acc, const Kahan* acc2) {
+  float s[2 * NV], c[2 * NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    s[2 * i] = acc[i].s;
+    c[2 * i] = acc[i].c;
+    s[2 * i + 1] = acc2[i].s;
+    c[2 * i + 1] = acc2[i].c;
+  }
+  block_sum_kahan_store<2 * NV>(s, c, a.partials + (uint64_t)blockIdx.x * 2 * NV);
+}
+
+template <int ILP>
+__global__ void __launch_bounds__(256) k_gbm_fused(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  Kahan acc[1], acc2[1];
+  const float s0 = a.f32.g_s0, diffusion = a.f32.g_diff, kdrift = a.f32.g_kdrift, strike = a.f32.strike;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
+    bool ok[ILP], neg[ILP];
+    PcgGen s[ILP];
+    Kahan w[ILP];
+    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+#pragma unroll 1
+    for (uint64_t k = 0; k < a.steps; ++k) {
+      float z[ILP];
+      normals<ILP>(s, z, c, zs, err);
+#pragma unroll
+      for (int j = 0; j < ILP; ++j) w[j].add(neg[j] ? -z[j] : z[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < ILP; ++j)
+      if (ok[j]) {
+        const float p = payoff_f32(s0 * expf(fmaf(diffusion, w[j].value(), kdrift)), strike, a.payoff);
+        acc[0].add(p);
+        acc2[0].add(p * p);
+      }
+  }
+  store_partials<1>(a, acc, acc2);
+  if (err) atomicOr(a.err, err);
+}
+
+template <int ILP>
+__global__ void __launch_bounds__(256) k_heston_fused(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  const float rho = f.h_rho, rho_comp = f.h_rho_comp, kappa_dt = f.h_kdt, theta = f.h_theta;
+  const float xi_sdt = f.h_xsdt, sdt = f.h_sdt, mu_dt = f.h_mudt, nhdt = f.h_nhdt, s0 = f.h_s0;
+  unsigned err = 0;
+  Kahan acc[1], acc2[1];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
+    bool ok[ILP], neg[ILP];
+    PcgGen s[ILP];
+    Kahan lg[ILP];
+    float v[ILP];
+    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+#pragma unroll
+    for (int j = 0; j < ILP; ++j) v[j] = f.h_v0;
+#pragma unroll 1
+    for (uint64_t k = 0; k < a.steps; ++k) {
+      float dw1[ILP], dz[ILP];
+      normals<ILP>(s, dw1, c, zs, err);
+      normals<ILP>(s, dz, c, zs, err);
+#pragma unroll
+      for (int j = 0; j < ILP; ++j) {
+        const float dw2 = fmaf(rho, dw1[j], rho_comp * dz[j]);
+        const float v_plus = fmaxf(v[j], 0.0f);
+        const float sqrt_v = sqrtf(v_plus);
+        v[j] += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
+        lg[j].add(fmaf(nhdt, v_plus, mu_dt) + sqrt_v * sdt * dw1[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < ILP; ++j)
+      if (ok[j]) {
+        const float p = payoff_f32(s0 * expf(lg[j].value()), f.strike, a.payoff);
+        acc[0].add(p);
+        acc2[0].add(p * p);
+      }
+  }
+  store_partials<1>(a, acc, acc2);
+  if (err) atomicOr(a.err, err);
+}
+
+template <int ILP>
+__global__ void __launch_bounds__(256) k_merton_fused(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  const float diffusion = f.m_diff, kdrift = f.m_kdrift, mu_j = f.m_mu_j, sigma_j = f.m_sigma_j, s0 = f.m_s0;
+  const uint64_t thr = a.merton.jump_thr;
+  unsigned err = 0;
+  Kahan acc[1], acc2[1];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
+    bool ok[ILP], neg[ILP];
+    PcgGen s[ILP];
+    Kahan w[ILP];
+    float jumps[ILP];
+    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+#pragma unroll
+    for (int j = 0; j < ILP; ++j) jumps[j] = 0.0f;
+#pragma unroll 1
+    for (uint64_t k = 0; k < a.steps; ++k) {
+      float z[ILP];
+      normals<ILP>(s, z, c, zs, err);
+#pragma unroll
+      for (int j = 0; j < ILP; ++j) {
+        w[j].add(z[j]);
+        if ((s[j].next() >> 11) < thr) jumps[j] += fmaf(sigma_j, normal_f32(s[j], c, zs, err), mu_j);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < ILP; ++j)
+      if (ok[j]) {
+        const float p = payoff_f32(s0 * expf(fmaf(diffusion, w[j].value(), kdrift) + jumps[j]), f.strike, a.payoff);
+        acc[0].add(p);
+        acc2[0].add(p * p);
+      }
+  }
+  store_partials<1>(a, acc, acc2);
+  if (err) atomicOr(a.err, err);
+}
+
+template <int NA, int ILP>
+__global__ void __launch_bounds__(256) k_multi_fused(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  unsigned err = 0;
+  Kahan acc[NA], acc2[NA];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
+    bool ok[ILP], neg[ILP];
+    PcgGen s[ILP];
+    Kahan w[ILP][NA];
+    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+#pragma unroll 1
+    for (uint64_t k = 0; k < a.steps; ++k) {
+#pragma unroll
+      for (int i = 0; i < NA; ++i) {
+        float z[ILP];
+        normals<ILP>(s, z, c, zs, err);
+#pragma unroll
+        for (int j = 0; j < ILP; ++j) w[j][i].add(neg[j] ? -z[j] : z[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < ILP; ++j)
+      if (ok[j]) {
+#pragma unroll
+        for (int i = 0; i < NA; ++i) {
+          float eps = 0.0f;
+#pragma unroll
+          for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[j][m].value(), eps);
+          const float p = payoff_f32(f.a_s0[i] * expf(fmaf(f.a_diff[i], eps, f.a_kdrift[i])), f.strike, a.payoff);
+          acc[i].add(p);
+          acc2[i].add(p * p);
+        }
+      }
+  }
+  store_partials<NA>(a, acc, acc2);
+  if (err) atomicOr(a.err, err);
+}
+
+// Tuning table: per model kind (gbm, heston, merton, multi-GBM with 1..4
+// assets) the block size, ILP and grid waves of the fused launch.
+FusedTune g_tune[kTuneSlots] = {{256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0},
+                                {256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0}};
+
+const void* fused_kernel(int slot, int ilp, int variant) {
+  if (variant == 0) {  // the per-path loop kernels (one path per thread at a time)
+    switch (slot) {
+      case 0: return (const void*)k_gbm_f32<false>;
+      case 1: return (const void*)k_heston_euler_f32<false>;
+      case 2: return (const void*)k_merton_f32<false>;
+      case 3: return (const void*)k_multi_gbm_f32<1, false>;
+      case 4: return (const void*)k_multi_gbm_f32<2, false>;
+      case 5: return (const void*)k_multi_gbm_f32<3, false>;
+      default: return (const void*)k_multi_gbm_f32<4, false>;
+    }
+  }
+  const bool two = ilp == 2;
+  switch (slot) {
+    case 0: return two ? (const void*)k_gbm_fused<2> : (const void*)k_gbm_fused<1>;
+    case 1: return two ? (const void*)k_heston_fused<2> : (const void*)k_heston_fused<1>;
+    case 2: return two ? (const void*)k_merton_fused<2> : (const void*)k_merton_fused<1>;
+    case 3: return two ? (const void*)k_multi_fused<1, 2> : (const void*)k_multi_fused<1, 1>;
+    case 4: return two ? (const void*)k_multi_fused<2, 2> : (const void*)k_multi_fused<2, 1>;
+    case 5: return two ? (const void*)k_multi_fused<3, 2> : (const void*)k_multi_fused<3, 1>;
+    default: return two ? (const void*)k_multi_fused<4, 2> : (const void*)k_multi_fused<4, 1>;
+  }
+}
+
 template <bool kStore>
 void launch_multi32(const PathLaunch& L, dim3 g, dim3 b, cudaStream_t st) {
   switch (L.multi.na) {
@@ -223,12 +457,46 @@ void launch_multi32(const PathLaunch& L, dim3 g, dim3 b, cudaStream_t st) {
 
 }  // namespace
 
+int tune_slot(int model, int na) {
+  if (model == kMultiGbm) return na >= 1 && na <= 4 ? 2 + na : -1;
+  return model == kGbm ? 0 : model == kHeston ? 1 : model == kMerton ? 2 : -1;
+}
+
+FusedTune get_fused_tune(int slot) {
+  return slot >= 0 && slot < kTuneSlots ? g_tune[slot] : FusedTune{256, 1, 1, 0};
+}
+
+int set_fused_tune(int slot, FusedTune t) {
+  if (slot < 0 || slot >= kTuneSlots) return -1;
+  if ((t.block != 64 && t.block != 128 && t.block != 256) || (t.ilp != 1 && t.ilp != 2) || t.waves < 1 ||
+      t.waves > 2 || (t.variant != 0 && t.variant != 1) || (t.variant == 0 && t.ilp != 1))
+    return -1;
+  g_tune[slot] = t;
+  return 0;
+}
+
 int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int b = 256;
   const bool store = L.out_f32 != nullptr;
+  const int slot = tune_slot(L.model, L.multi.na);
+  if (!store && slot >= 0 && !(L.model == kHeston && L.heston.scheme != 0)) {
+    // fused pricing: tuned block size, ILP and waves of resident blocks
+    const FusedTune t = g_tune[slot];
+    const void* fn = fused_kernel(slot, t.ilp, t.variant);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.block, 0) != cudaSuccess || per_sm < 1)
+      per_sm = 1;
+    uint64_t g = (L.rows + (uint64_t)t.block * t.ilp - 1) / ((uint64_t)t.block * t.ilp);
+    const uint64_t cap = (uint64_t)sms * per_sm * t.waves;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    void* args[] = {(void*)&L};
+    if (cudaLaunchKernel(fn, dim3((unsigned)g), dim3(t.block), args, 0, st) != cudaSuccess) return -1;
+    return (int)g;
+  }
+  const int b = 256;
   // Persistent grid: exactly the blocks that are resident at once, so the
   // grid-stride loop gives every thread the same number of paths (+-1) in a
   // single wave instead of a partial second wave of blocks.

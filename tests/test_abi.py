@@ -220,3 +220,23 @@ def test_serving_arena_host_logic(stocha):
     P = ctypes.POINTER(ctypes.c_int64)
     lib.stocha_debug_arena(cap, ops.ctypes.data_as(P), 4, res.ctypes.data_as(P))
     assert res[0] == 0 and res[1] == cap // 2 and res[3] == -1
+
+
+def test_tune_table_host_logic(stocha):
+    """The fused-kernel launch-shape table: valid shapes are installed and read
+    back, invalid ones are refused with ValueError (no GPU involved)."""
+    before = stocha.tune_get("gbm")
+    try:
+        stocha.tune_set("gbm", 128, 2, 2, variant=1)
+        got = stocha.tune_get("gbm")
+        assert (got["block"], got["ilp"], got["waves"], got["variant"]) == (128, 2, 2, 1)
+        for bad in [(512, 1, 1, 1), (256, 3, 1, 1), (256, 1, 0, 1), (256, 1, 3, 1), (256, 2, 1, 0), (256, 1, 1, 2)]:
+            with pytest.raises(ValueError):
+                stocha.tune_set("gbm", bad[0], bad[1], bad[2], variant=bad[3])
+        with pytest.raises(ValueError):
+            stocha.tune_get("multi_gbm", 9)  # more than 4 assets: generic kernel, no table slot
+        stocha.tune_set("multi_gbm", 64, 1, 2, variant=0, n_assets=3)
+        assert stocha.tune_get("multi_gbm", 3)["block"] == 64
+    finally:
+        stocha.tune_set("gbm", before["block"], before["ilp"], before["waves"], variant=before["variant"])
+        stocha.tune_set("multi_gbm", 256, 1, 1, variant=0, n_assets=3)

@@ -113,3 +113,37 @@ def test_fp32_materialised_close_to_fp64(stocha):
     _lib.check(lib.stocha_ctx_sync(None))
     a, b = d64.cpu().numpy(), d32.cpu().double().numpy()
     assert np.max(np.abs(a - b) / a) < 1e-4
+
+
+@pytest.mark.parametrize("model", ["gbm", "heston", "merton", "multi_gbm"])
+def test_every_tuned_launch_shape(stocha, model):
+    """Each launch shape the autotuner can install (threads per block, paths
+    per thread in lockstep, grid waves) draws the same values: the FP32 fused
+    price stays within 1e-5 of the FP64 plain price for all eighteen, on odd
+    path counts (the lockstep tail) and antithetic multi-GBM; then a real
+    autotune installs one of them."""
+    if model == "multi_gbm":
+        p = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.15],
+                 corr=[[1, .6, .3], [.6, 1, .5], [.3, .5, 1]], t=1.0)
+        na = 3
+    else:
+        p, na = MODELS[model], 0
+    before = stocha.tune_get(model, na)
+    try:
+        for n in (1, 777, 100_003):
+            kw = dict(strike=100.0, payoff="put", steps=50, n_paths=n, seed=9)
+            want = stocha.price_european(model, p, precision="fp64", **kw)
+            for block in (64, 128, 256):
+                for variant, ilp in ((0, 1), (1, 1), (1, 2)):
+                    for waves in (1, 2):
+                        stocha.tune_set(model, block, ilp, waves, variant=variant, n_assets=na)
+                        got = stocha.price_european(model, p, precision="fp32", **kw)
+                        pairs = zip(got, want) if model == "multi_gbm" else [(got, want)]
+                        for (g, _), (w, _) in pairs:
+                            assert abs(g - w) <= 1e-5 * max(abs(w), 1e-3), (n, block, ilp, waves, g, w)
+        t = stocha.autotune(model, p, steps=50, n_paths=200_000, reps=2)
+        assert t["candidates"] == 18 and t["ms_best"] <= t["ms_default"] * 1.0001
+        assert stocha.tune_get(model, na)["block"] == t["block"]
+    finally:
+        stocha.tune_set(model, before["block"], before["ilp"], before["waves"], variant=before["variant"],
+                        n_assets=na)
