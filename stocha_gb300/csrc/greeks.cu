@@ -254,16 +254,23 @@ __global__ void __launch_bounds__(256) k_greeks(const GreeksLaunch g) {
   if (err) atomicOr(g.err, err);
 }
 
-// One thread per instance: add its items' partials in order.
-__global__ void k_greeks_finish(const GreeksLaunch g) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// One block per instance: thread j adds the instance's items j, j + 256, ...
+// in order, then a fixed block tree; the totals depend only on the
+// instance's own items, never on what else is in the launch.
+__global__ void __launch_bounds__(256) k_greeks_finish(const GreeksLaunch g) {
+  const int i = blockIdx.x;
   if (i >= g.n_inst) return;
   const GInst& I = g.inst[i];
   const uint64_t items = (I.n_paths + I.chunk - 1) / I.chunk;
-  double s[kGreekAcc] = {0};
-  for (uint64_t it = 0; it < items; ++it)
-    for (int j = 0; j < kGreekAcc; ++j) s[j] += g.item_part[(I.item_begin + it) * kGreekAcc + j];
-  for (int j = 0; j < kGreekAcc; ++j) g.inst_sums[(uint64_t)i * kGreekAcc + j] = s[j];
+  double s[kGreekAcc];
+#pragma unroll
+  for (int j = 0; j < kGreekAcc; ++j) s[j] = 0.0;
+  for (uint64_t it = threadIdx.x; it < items; it += blockDim.x) {
+    const double* p = g.item_part + (I.item_begin + it) * kGreekAcc;
+#pragma unroll
+    for (int j = 0; j < kGreekAcc; ++j) s[j] += p[j];
+  }
+  block_sum_n_store<kGreekAcc>(s, g.inst_sums + (uint64_t)i * kGreekAcc);
 }
 
 }  // namespace
@@ -277,7 +284,7 @@ void launch_greeks_batch(const GreeksLaunch& g, cudaStream_t st) {
   if (blocks > g.total_items || g.direct) blocks = g.total_items ? g.total_items : 1;
   if (!g.direct) cudaMemsetAsync(g.counter, 0, sizeof(unsigned long long), st);
   k_greeks<<<(unsigned)blocks, 256, 0, st>>>(g);
-  k_greeks_finish<<<(g.n_inst + 127) / 128, 128, 0, st>>>(g);
+  if (g.n_inst > 0) k_greeks_finish<<<g.n_inst, 256, 0, st>>>(g);
 }
 
 }  // namespace stocha
