@@ -361,6 +361,28 @@ def bench_extras(stocha, torch, cores, skip_cpu):
         "fp32_vs_fp64_rel_err_median": dict(zip(names, np.median(rel, axis=0).tolist())),
         "fp32_vs_fp64_rel_err_max": dict(zip(names, np.max(rel, axis=0).tolist())),
         "fp64_sample": f"{len(sample)} instances (every 32nd) revalued scenario by scenario in FP64"}
+    # -- exotic Monte Carlo (barrier / Asian / lookback), FP64, 1e6 x 252
+    ex = {"workload": "1e6 paths x 252 steps, s=k=100 r=.05 sigma=.2 t=1, FP64 Monte Carlo (reference arithmetic)"}
+    cases = [("barrier_uo_call_h120", lambda n: stocha.barrier_price(100, 100, .05, .2, 1., 120, method="mc",
+                                                                     n_paths=n, n_steps=252),
+              lambda n: O.barrier_mc(100, 100, .05, .2, 1., 120, n_paths=n, n_steps=252, threads=cores)),
+             ("asian_arith_fixed_call_cv", lambda n: stocha.asian_price(100, 100, .05, .2, 1., method="mc", n_paths=n),
+              None),
+             ("lookback_floating_call", lambda n: stocha.lookback_price(100, .05, .2, 1., method="mc", n_paths=n),
+              lambda n: O.lookback_mc(100, .05, .2, 1., n_paths=n, threads=cores))]
+    for name, gpu, cpu in cases:
+        gpu(10_000)
+        t0 = time.perf_counter()
+        price = gpu(1_000_000)
+        dt = time.perf_counter() - t0
+        row = {"price": price, "ms": dt * 1e3, "path_steps_per_s": 1e6 * 252 / dt}
+        if cpu is not None and not skip_cpu:
+            t0 = time.perf_counter()
+            cpu(50_000)
+            row["cpu_path_steps_per_s"] = 5e4 * 252 / (time.perf_counter() - t0)
+            row["cpu_cores"] = cores
+        ex[name] = row
+    res["exotics_mc"] = ex
     # -- config 5: the serving loop
     res["config5_serving"] = bench_serving(stocha)
     return res

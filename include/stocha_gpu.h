@@ -243,6 +243,27 @@ int stocha_rng_from_state(const char* json, stocha_rng* out);
  * check the device generator against the reference bit for bit). */
 int stocha_rng_raw_u64(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, uint64_t* out);
 
+/* -------------------------------------------------------- exotic options
+ * replace barrier_price, asian_price, lookback_price (src/lib.rs:1549-1870;
+ * src/finance/barrier.rs, asian.rs, lookback.rs).  Same argument checks and
+ * messages; method "auto" / "analytical" / "mc".  The closed forms run on
+ * the host (they are a few hundred flops); "mc" (and "auto" where the
+ * reference falls back to it) runs the FP64 Monte Carlo kernel on the
+ * device with the reference's streams.  Optional arguments: n_monitoring < 0
+ * is None; running_avg, time_elapsed, running_max, running_min NaN is None. */
+int stocha_barrier_price(stocha_ctx* ctx, double s, double k, double r, double sigma, double t, double barrier,
+                         const char* barrier_type, const char* option_type, double q, uint64_t n_paths,
+                         uint64_t n_steps, uint64_t seed, const char* method, int32_t n_monitoring, double rebate,
+                         int32_t rebate_at_hit, double* price);
+int stocha_asian_price(stocha_ctx* ctx, double s, double k, double r, double sigma, double t, uint64_t n_steps,
+                       const char* average_type, const char* strike_type, const char* option_type, double q,
+                       uint64_t n_paths, uint64_t seed, const char* method, double running_avg, double time_elapsed,
+                       double* price);
+int stocha_lookback_price(stocha_ctx* ctx, double s, double r, double sigma, double t, uint64_t n_steps,
+                          const char* strike_type, const char* option_type, double k, double q, uint64_t n_paths,
+                          uint64_t seed, const char* method, double running_max, double running_min,
+                          double* price);
+
 /* ------------------------------------------------------------- autotuner
  * No counterpart in the reference.  The fused FP32 pricing kernels have a
  * launch shape per model kind: the kernel form (variant 0: one path per

@@ -68,6 +68,15 @@ def lib():
         L.oracle_greeks_fd.argtypes = [_int, _pdbl, _int, _int, _dbl, _u64, _u64, _pint, _int, _u64, _dbl, _int,
                                        _pdbl]
         L.oracle_greeks_pathwise.argtypes = [_dbl] * 5 + [_int, _u64, _u64, _pint, _int, _u64, _int, _pdbl]
+        L.oracle_barrier_mc.argtypes = [_dbl] * 7 + [_int, _int, _int, _dbl, _int, _u64, _u64, _u64, _int]
+        L.oracle_barrier_mc.restype = _dbl
+        L.oracle_asian_paths.argtypes = [_dbl] * 6 + [_u64, _int, _int, _u64, _u64, _int, _pdbl, _pdbl]
+        L.oracle_asian_estimate.argtypes = [_pdbl, _pdbl, _u64, _int, _dbl, _dbl]
+        L.oracle_asian_estimate.restype = _dbl
+        L.oracle_asian_floating_seasoned.argtypes = [_dbl] * 5 + [_u64, _int, _int, _dbl, _dbl, _u64, _u64, _int]
+        L.oracle_asian_floating_seasoned.restype = _dbl
+        L.oracle_lookback_mc.argtypes = [_dbl] * 6 + [_u64, _int, _int, _dbl, _dbl, _u64, _u64, _int]
+        L.oracle_lookback_mc.restype = _dbl
         _lib = L
     return _lib
 
@@ -220,3 +229,50 @@ def greeks_pathwise(s0, r, sigma, t, strike, is_call, n_paths, n_steps, greeks, 
     lib().oracle_greeks_pathwise(s0, r, sigma, t, strike, int(is_call), n_paths, n_steps, _p(codes, _pint),
                                  len(greeks), seed, threads, _p(out))
     return {g: float(v) for g, v in zip(greeks, out)}
+
+
+# ---------------------------------------------------------- exotic MC ---
+_DIR = {"up-and-out": (0, 0), "uo": (0, 0), "up-and-in": (0, 1), "ui": (0, 1), "down-and-out": (1, 0),
+        "do": (1, 0), "down-and-in": (1, 1), "di": (1, 1)}
+
+
+def barrier_mc(s, k, r, sigma, t, barrier, barrier_type="up-and-out", option_type="call", q=0.0, n_paths=100_000,
+               n_steps=252, seed=42, rebate=0.0, rebate_at_hit=False, threads=0):
+    """barrier.rs:286-372 barrier_mc."""
+    d, kin = _DIR[barrier_type]
+    return lib().oracle_barrier_mc(s, k, r, q, sigma, t, barrier, d, kin, int(option_type == "call"), rebate,
+                                   int(rebate_at_hit), n_paths, n_steps, seed, threads)
+
+
+def asian_paths(s, k, r, sigma, t, n_steps, strike_type="fixed", option_type="call", q=0.0, n_paths=100_000,
+                seed=42, threads=0):
+    """Per-path (arithmetic, geometric) payoffs of asian.rs:143-268."""
+    a = np.empty(n_paths)
+    g = np.empty(n_paths)
+    lib().oracle_asian_paths(s, k, r, q, sigma, t, n_steps, int(strike_type == "floating"),
+                             int(option_type == "call"), n_paths, seed, threads, _p(a), _p(g))
+    return a, g
+
+
+def asian_estimate(arith, geo, use_cv, geo_analytical, discount):
+    """asian.rs:270-289: the control-variate (or plain) estimator."""
+    a = np.ascontiguousarray(arith, np.float64)
+    g = np.ascontiguousarray(geo, np.float64)
+    return lib().oracle_asian_estimate(_p(a), _p(g), a.size, int(use_cv), geo_analytical, discount)
+
+
+def asian_floating_seasoned(s, r, sigma, t, n_steps, average_type, option_type, a_spent, t1, q=0.0,
+                            n_paths=100_000, seed=42, threads=0):
+    """asian.rs:292-352 asian_mc_floating_seasoned."""
+    return lib().oracle_asian_floating_seasoned(s, r, q, sigma, t, n_steps, int(average_type == "geometric"),
+                                                int(option_type == "call"), a_spent, t1, n_paths, seed, threads)
+
+
+def lookback_mc(s, r, sigma, t, n_steps=252, strike_type="floating", option_type="call", k=0.0, q=0.0,
+                n_paths=100_000, seed=42, running_max=None, running_min=None, threads=0):
+    """lookback.rs:158-210 lookback_mc."""
+    nan = float("nan")
+    return lib().oracle_lookback_mc(s, k, r, q, sigma, t, n_steps, int(strike_type == "fixed"),
+                                    int(option_type == "call"), nan if running_max is None else running_max,
+                                    nan if running_min is None else running_min, n_paths, seed, threads)
+

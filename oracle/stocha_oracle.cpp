@@ -746,3 +746,195 @@ ORACLE_API void oracle_greeks_pathwise(double s0, double r, double sigma, double
   }
 }
 
+
+// ------------------------------------------------------ exotic MC -------
+// src/finance/barrier.rs:286-372 (barrier_mc, rebate_path_pv), asian.rs:143-290
+// and 292-352 (asian_mc, asian_mc_floating_seasoned), lookback.rs:158-210
+// (lookback_mc).  Per path: Pcg64Dxsm::new(seed) advanced by path * block,
+// block = (steps + 1024) * 2; GBM step s *= exp(drift + diffusion * z).
+// The reference adds the per-chunk sums with a Rayon reduction; here the paths
+// are added in order (the sums differ only in summation order).
+namespace {
+
+double rebate_path_pv(int kind_in, int at_hit, double rebate, double r, int hit_step, uint64_t steps, double dt) {
+  const bool knocked = hit_step >= 0;  // barrier.rs:379-403
+  if (!kind_in && at_hit) return knocked ? rebate * std::exp(-r * ((double)hit_step * dt)) : 0.0;
+  if (!kind_in) return knocked ? rebate * std::exp(-r * ((double)steps * dt)) : 0.0;
+  return knocked ? 0.0 : rebate * std::exp(-r * ((double)steps * dt));
+}
+
+inline double vanilla_intrinsic(double s, double k, int is_call) {
+  return is_call ? std::max(s - k, 0.0) : std::max(k - s, 0.0);
+}
+
+}  // namespace
+
+// direction: 0 up, 1 down; kind_in: 1 knock-in, 0 knock-out.
+ORACLE_API double oracle_barrier_mc(double s0, double k, double r, double q, double sigma, double t, double barrier,
+                                    int direction, int kind_in, int is_call, double rebate, int rebate_at_hit,
+                                    uint64_t n_paths, uint64_t steps, uint64_t seed, int threads) {
+  const double dt = t / (double)steps;
+  const double drift = (r - q - 0.5 * sigma * sigma) * dt;
+  const double diffusion = sigma * std::sqrt(dt);
+  const double discount = std::exp(-r * t);
+  const u128 block = ((u128)steps + 1024) * 2;
+  const bool already_hit = direction == 0 ? s0 >= barrier : s0 <= barrier;
+  std::vector<double> pay(n_paths);
+  parallel_for(n_paths, threads, [&](uint64_t a, uint64_t b) {
+    for (uint64_t i = a; i < b; ++i) {
+      Pcg g = path_stream(seed, i, block);
+      double s = s0;
+      int hit = -1;
+      if (already_hit) {
+        hit = 0;
+      } else {
+        for (uint64_t st = 1; st <= steps; ++st) {
+          const double z = zig_normal(g);
+          s *= std::exp(drift + diffusion * z);
+          if (direction == 0 ? s >= barrier : s <= barrier) {
+            hit = (int)st;
+            break;
+          }
+        }
+      }
+      const bool knocked = hit >= 0;
+      if (knocked && kind_in && (uint64_t)hit < steps)
+        for (uint64_t st = (uint64_t)hit; st < steps; ++st) {
+          const double z = zig_normal(g);
+          s *= std::exp(drift + diffusion * z);
+        }
+      const double opt = kind_in ? (knocked ? vanilla_intrinsic(s, k, is_call) : 0.0)
+                                 : (knocked ? 0.0 : vanilla_intrinsic(s, k, is_call));
+      const double rpv = rebate == 0.0 ? 0.0 : rebate_path_pv(kind_in, rebate_at_hit, rebate, r, hit, steps, dt);
+      pay[i] = opt + rpv / discount;
+    }
+  });
+  double total = 0.0;
+  for (double v : pay) total += v;
+  return discount * total / (double)n_paths;
+}
+
+// Per-path (arithmetic, geometric) payoffs of asian_mc (asian.rs:225-268):
+// fixed (strike_floating = 0) or floating strike, call or put.
+ORACLE_API void oracle_asian_paths(double s0, double k, double r, double q, double sigma, double t, uint64_t steps,
+                                   int strike_floating, int is_call, uint64_t n_paths, uint64_t seed, int threads,
+                                   double* arith, double* geo) {
+  const double dt = t / (double)steps;
+  const double drift = (r - q - 0.5 * sigma * sigma) * dt;
+  const double diffusion = sigma * std::sqrt(dt);
+  const u128 block = ((u128)steps + 1024) * 2;
+  parallel_for(n_paths, threads, [&](uint64_t a, uint64_t b) {
+    for (uint64_t i = a; i < b; ++i) {
+      Pcg g = path_stream(seed, i, block);
+      double s = s0, sum_arith = 0.0, sum_log = 0.0;
+      for (uint64_t st = 0; st < steps; ++st) {
+        const double z = zig_normal(g);
+        s *= std::exp(drift + diffusion * z);
+        sum_arith += s;
+        sum_log += std::log(s);
+      }
+      const double avg_a = sum_arith / (double)steps;
+      const double avg_g = std::exp(sum_log / (double)steps);
+      if (!strike_floating) {
+        arith[i] = is_call ? std::max(avg_a - k, 0.0) : std::max(k - avg_a, 0.0);
+        geo[i] = is_call ? std::max(avg_g - k, 0.0) : std::max(k - avg_g, 0.0);
+      } else {
+        arith[i] = is_call ? std::max(s - avg_a, 0.0) : std::max(avg_a - s, 0.0);
+        geo[i] = is_call ? std::max(s - avg_g, 0.0) : std::max(avg_g - s, 0.0);
+      }
+    }
+  });
+}
+
+// asian_mc's estimator (asian.rs:270-289): geometric control variate for the
+// arithmetic fixed-strike case (use_cv), else the plain mean.
+ORACLE_API double oracle_asian_estimate(const double* arith, const double* geo, uint64_t n, int use_cv,
+                                        double geo_analytical, double discount) {
+  if (use_cv && n > 1) {
+    double ma = 0.0, mg = 0.0;
+    for (uint64_t i = 0; i < n; ++i) ma += arith[i];
+    ma /= (double)n;
+    for (uint64_t i = 0; i < n; ++i) mg += geo[i];
+    mg /= (double)n;
+    double cov = 0.0, vg = 0.0;
+    for (uint64_t i = 0; i < n; ++i) {
+      cov += (arith[i] - ma) * (geo[i] - mg);
+      vg += (geo[i] - mg) * (geo[i] - mg);
+    }
+    const double beta = vg > 1e-30 ? cov / vg : 0.0;
+    const double geo_mc = discount * mg;
+    return std::max(discount * ma - beta * (geo_mc - geo_analytical), 0.0);
+  }
+  double m = 0.0;
+  for (uint64_t i = 0; i < n; ++i) m += arith[i];
+  return std::max(discount * (m / (double)n), 0.0);
+}
+
+// asian_mc_floating_seasoned (asian.rs:292-352): remaining-period paths with
+// the spent average blended in; geometric = 1 for the geometric average.
+ORACLE_API double oracle_asian_floating_seasoned(double s0, double r, double q, double sigma, double t, uint64_t n_steps,
+                                                 int geometric, int is_call, double a_spent, double t1,
+                                                 uint64_t n_paths, uint64_t seed, int threads) {
+  const double remaining = t - t1;
+  uint64_t nr = (uint64_t)std::llround((double)n_steps * remaining / t);
+  if (nr < 1) nr = 1;
+  const double dt = remaining / (double)nr;
+  const double drift = (r - q - 0.5 * sigma * sigma) * dt;
+  const double diffusion = sigma * std::sqrt(dt);
+  const double discount = std::exp(-r * remaining);
+  const double w_spent = t1 / t, w_remain = remaining / t;
+  const u128 block = ((u128)nr + 1024) * 2;
+  std::vector<double> pay(n_paths);
+  parallel_for(n_paths, threads, [&](uint64_t a, uint64_t b) {
+    for (uint64_t i = a; i < b; ++i) {
+      Pcg g = path_stream(seed, i, block);
+      double s = s0, sum_arith = 0.0, sum_log = 0.0;
+      for (uint64_t st = 0; st < nr; ++st) {
+        const double z = zig_normal(g);
+        s *= std::exp(drift + diffusion * z);
+        sum_arith += s;
+        sum_log += std::log(s);
+      }
+      const double avg_rem = geometric ? std::exp(sum_log / (double)nr) : sum_arith / (double)nr;
+      const double avg_t = geometric ? std::exp(std::log(a_spent) * w_spent + std::log(avg_rem) * w_remain)
+                                     : w_spent * a_spent + w_remain * avg_rem;
+      pay[i] = is_call ? std::max(s - avg_t, 0.0) : std::max(avg_t - s, 0.0);
+    }
+  });
+  double total = 0.0;
+  for (double v : pay) total += v;
+  return discount * total / (double)n_paths;
+}
+
+// lookback_mc (lookback.rs:158-210); running_max / running_min: NaN = none.
+ORACLE_API double oracle_lookback_mc(double s0, double k, double r, double q, double sigma, double t, uint64_t steps,
+                                     int strike_fixed, int is_call, double running_max, double running_min,
+                                     uint64_t n_paths, uint64_t seed, int threads) {
+  const double dt = t / (double)steps;
+  const double drift = (r - q - 0.5 * sigma * sigma) * dt;
+  const double diffusion = sigma * std::sqrt(dt);
+  const double discount = std::exp(-r * t);
+  const u128 block = ((u128)steps + 1024) * 2;
+  const double m0 = std::max(std::isnan(running_max) ? s0 : running_max, s0);
+  const double n0 = std::min(std::isnan(running_min) ? s0 : running_min, s0);
+  std::vector<double> pay(n_paths);
+  parallel_for(n_paths, threads, [&](uint64_t a, uint64_t b) {
+    for (uint64_t i = a; i < b; ++i) {
+      Pcg g = path_stream(seed, i, block);
+      double s = s0, mx = m0, mn = n0;
+      for (uint64_t st = 0; st < steps; ++st) {
+        const double z = zig_normal(g);
+        s *= std::exp(drift + diffusion * z);
+        if (s > mx) mx = s;
+        if (s < mn) mn = s;
+      }
+      if (!strike_fixed)
+        pay[i] = is_call ? s - mn : mx - s;
+      else
+        pay[i] = is_call ? std::max(mx - k, 0.0) : std::max(k - mn, 0.0);
+    }
+  });
+  double total = 0.0;
+  for (double v : pay) total += v;
+  return discount * total / (double)n_paths;
+}

@@ -291,3 +291,57 @@ def _alloc(n_paths, cols, plausible, n_assets=None):
         return np.empty(shape, np.float64)
     shape = (n_paths, cols) if n_assets is None else (n_paths, cols, n_assets)
     return np.empty(shape, np.float64)
+
+
+# ------------------------------------------------------- exotic options ---
+def _opt_f64(x, name):
+    return float("nan") if x is None else _f64(x, name)
+
+
+def barrier_price(s, k, r, sigma, t, barrier, barrier_type="up-and-out", option_type="call", q=0.0,
+                  n_paths=100_000, n_steps=252, seed=42, method="auto", n_monitoring=None, rebate=0.0,
+                  rebate_at_hit=False):
+    """lib.rs:1549-1641: barrier option price (analytical or Monte Carlo)."""
+    vals = [_f64(v, nm) for v, nm in zip((s, k, r, sigma, t, barrier), ("s", "k", "r", "sigma", "t", "barrier"))]
+    barrier_type, option_type = _str(barrier_type, "barrier_type"), _str(option_type, "option_type")
+    q = _f64(q, "q")
+    n_paths, n_steps, seed = _usize(n_paths, "n_paths"), _usize(n_steps, "n_steps"), _usize(seed, "seed")
+    method = _str(method, "method")
+    n_mon = -1 if n_monitoring is None else _uint(n_monitoring, 2**32 - 1, "n_monitoring")
+    rebate, rebate_at_hit = _f64(rebate, "rebate"), _bool(rebate_at_hit, "rebate_at_hit")
+    out = ctypes.c_double(0.0)
+    check(load().stocha_barrier_price(None, *vals, barrier_type.encode(), option_type.encode(), q, n_paths, n_steps,
+                                      seed, method.encode(), n_mon, rebate, int(rebate_at_hit), ctypes.byref(out)))
+    return float(out.value)
+
+
+def asian_price(s, k, r, sigma, t, n_steps=252, average_type="arithmetic", strike_type="fixed", option_type="call",
+                q=0.0, n_paths=100_000, seed=42, method="auto", running_avg=None, time_elapsed=None):
+    """lib.rs:1643-1757: Asian option price (Kemna-Vorst or Monte Carlo)."""
+    vals = [_f64(v, nm) for v, nm in zip((s, k, r, sigma, t), ("s", "k", "r", "sigma", "t"))]
+    n_steps = _usize(n_steps, "n_steps")
+    average_type, strike_type = _str(average_type, "average_type"), _str(strike_type, "strike_type")
+    option_type, q = _str(option_type, "option_type"), _f64(q, "q")
+    n_paths, seed, method = _usize(n_paths, "n_paths"), _usize(seed, "seed"), _str(method, "method")
+    out = ctypes.c_double(0.0)
+    check(load().stocha_asian_price(None, *vals, n_steps, average_type.encode(), strike_type.encode(),
+                                    option_type.encode(), q, n_paths, seed, method.encode(),
+                                    _opt_f64(running_avg, "running_avg"), _opt_f64(time_elapsed, "time_elapsed"),
+                                    ctypes.byref(out)))
+    return float(out.value)
+
+
+def lookback_price(s, r, sigma, t, n_steps=252, strike_type="floating", option_type="call", k=0.0, q=0.0,
+                   n_paths=100_000, seed=42, method="auto", running_max=None, running_min=None):
+    """lib.rs:1759-1870: lookback option price (GSG / Conze-Viswanathan or Monte Carlo)."""
+    vals = [_f64(v, nm) for v, nm in zip((s, r, sigma, t), ("s", "r", "sigma", "t"))]
+    n_steps = _usize(n_steps, "n_steps")
+    strike_type, option_type = _str(strike_type, "strike_type"), _str(option_type, "option_type")
+    k, q = _f64(k, "k"), _f64(q, "q")
+    n_paths, seed, method = _usize(n_paths, "n_paths"), _usize(seed, "seed"), _str(method, "method")
+    out = ctypes.c_double(0.0)
+    check(load().stocha_lookback_price(None, *vals, n_steps, strike_type.encode(), option_type.encode(), k, q, n_paths,
+                                       seed, method.encode(), _opt_f64(running_max, "running_max"),
+                                       _opt_f64(running_min, "running_min"), ctypes.byref(out)))
+    return float(out.value)
+

@@ -29,13 +29,14 @@ CUDA_UNITS = {
     "paths_f32.cu": [],
     "rng.cu": ["--fmad=false"],
     "lsmc.cu": [],
+    "exotics.cu": ["--fmad=false"],
     "greeks.cu": [],
     "batch.cu": [],
     "peaks.cu": [],
     "noalloc.cu": [],
 }
 HOST_UNITS = ["api.cpp", "rng_host.cpp", "lsmc_host.cpp", "greeks_host.cpp", "batch_host.cpp", "serve.cpp",
-              "hostcopy.cpp"]
+              "hostcopy.cpp", "exotics_host.cpp"]
 
 
 def _cuda_home() -> str:

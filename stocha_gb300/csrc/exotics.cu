@@ -1,0 +1,163 @@
+// Exotic Monte Carlo payoffs on GBM paths, FP64 (the reference's arithmetic):
+//   barrier   src/finance/barrier.rs:286-403 (barrier_mc, rebate_path_pv)
+//   asian     src/finance/asian.rs:143-290 (asian_mc: per-path arithmetic and
+//             geometric payoffs; the control-variate estimator runs as two
+//             device reductions) and :292-352 (asian_mc_floating_seasoned)
+//   lookback  src/finance/lookback.rs:158-210 (lookback_mc)
+// Every path has its own stream, Pcg64Dxsm::new(seed) advanced by
+// path * (steps + 1024) * 2, and the GBM step s *= exp(drift + diffusion * z)
+// with the kernels' table-driven exponential.  The running log price of the
+// geometric average is carried as a sum of the step exponents (ln s_k =
+// ln s0 + sum of (drift + diffusion * z)), equal to the reference's ln(s_k)
+// to rounding.  Payoffs never leave registers; per-block FP64 sums (or, for
+// the Asian estimator, the per-path payoff pair) go to device memory.
+#include <cuda_runtime.h>
+
+#include "exotics_kernels.h"
+#include "mc_device.cuh"
+#include "reduce.cuh"
+
+namespace stocha {
+namespace {
+
+__device__ __forceinline__ double intrinsic(double s, double k, int is_call) {
+  return is_call ? fmax(s - k, 0.0) : fmax(k - s, 0.0);
+}
+
+// barrier.rs:379-403: rebate paid at the hit time (knock-out, at_hit), at
+// expiry on a hit (knock-out), or at expiry without a hit (knock-in).
+__device__ __forceinline__ double rebate_pv(const ExoticLaunch& a, int hit) {
+  const bool knocked = hit >= 0;
+  if (!a.kind_in && a.rebate_at_hit) return knocked ? a.rebate * exp(-a.r * ((double)hit * a.dt)) : 0.0;
+  if (!a.kind_in) return knocked ? a.rebate * exp(-a.r * ((double)a.steps * a.dt)) : 0.0;
+  return knocked ? 0.0 : a.rebate * exp(-a.r * ((double)a.steps * a.dt));
+}
+
+__global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  double sum = 0.0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    PcgGen g{pcg_path_state(a.ss, i), a.ss.inc_lo, a.ss.inc_hi};
+    double s = a.s0;
+    if (a.kind == kExoBarrier) {
+      int hit = -1;
+      if (a.already_hit) {
+        hit = 0;
+      } else {
+        for (uint64_t st = 1; st <= a.steps; ++st) {
+          const double z = normal_f64(g, c, zs, err);
+          s = mul_exp(s, a.drift + a.diffusion * z, zs);
+          if (a.direction == 0 ? s >= a.barrier : s <= a.barrier) {
+            hit = (int)st;
+            break;
+          }
+        }
+      }
+      const bool knocked = hit >= 0;
+      if (knocked && a.kind_in && (uint64_t)hit < a.steps)  // drive a knocked-in path to T
+        for (uint64_t st = (uint64_t)hit; st < a.steps; ++st) {
+          const double z = normal_f64(g, c, zs, err);
+          s = mul_exp(s, a.drift + a.diffusion * z, zs);
+        }
+      const double opt = a.kind_in ? (knocked ? intrinsic(s, a.k, a.is_call) : 0.0)
+                                   : (knocked ? 0.0 : intrinsic(s, a.k, a.is_call));
+      const double rpv = a.rebate == 0.0 ? 0.0 : rebate_pv(a, hit);
+      sum += opt + rpv / a.discount;
+    } else if (a.kind == kExoLookback) {
+      double mx = a.m0, mn = a.n0;
+      for (uint64_t st = 0; st < a.steps; ++st) {
+        const double z = normal_f64(g, c, zs, err);
+        s = mul_exp(s, a.drift + a.diffusion * z, zs);
+        if (s > mx) mx = s;
+        if (s < mn) mn = s;
+      }
+      sum += a.strike_fixed ? (a.is_call ? fmax(mx - a.k, 0.0) : fmax(a.k - mn, 0.0))
+                            : (a.is_call ? s - mn : mx - s);
+    } else {  // Asian: plain (per-path pair) or floating seasoned (block sum)
+      double sum_arith = 0.0, sum_log = 0.0, lg = a.log_s0;
+      for (uint64_t st = 0; st < a.steps; ++st) {
+        const double z = normal_f64(g, c, zs, err);
+        const double x = a.drift + a.diffusion * z;
+        s = mul_exp(s, x, zs);
+        lg += x;
+        sum_arith += s;
+        sum_log += lg;
+      }
+      const double nsteps = (double)a.steps;
+      const double avg_a = sum_arith / nsteps;
+      const double avg_g = exp(sum_log / nsteps);
+      if (a.kind == kExoAsian) {
+        double pa, pg;
+        if (!a.strike_floating) {
+          pa = intrinsic(avg_a, a.k, a.is_call);
+          pg = intrinsic(avg_g, a.k, a.is_call);
+        } else {
+          pa = a.is_call ? fmax(s - avg_a, 0.0) : fmax(avg_a - s, 0.0);
+          pg = a.is_call ? fmax(s - avg_g, 0.0) : fmax(avg_g - s, 0.0);
+        }
+        a.arith[i] = pa;
+        a.geo[i] = pg;
+      } else {  // kExoAsianSeasoned (floating strike)
+        const double avg_rem = a.geometric ? avg_g : avg_a;
+        const double avg_t = a.geometric ? exp(log(a.a_spent) * a.w_spent + log(avg_rem) * a.w_remain)
+                                         : a.w_spent * a.a_spent + a.w_remain * avg_rem;
+        sum += a.is_call ? fmax(s - avg_t, 0.0) : fmax(avg_t - s, 0.0);
+      }
+    }
+  }
+  if (a.kind != kExoAsian) block_sum2_store(sum, 0.0, a.partials + 2 * (uint64_t)blockIdx.x);
+  if (err) atomicOr(a.err, err);
+}
+
+// Sums over the Asian payoff pairs: mode 0 {sum a, sum g}; mode 1, with the
+// means m = {ma, mg}: {sum (a - ma)(g - mg), sum (g - mg)^2} (asian.rs:270-281).
+__global__ void __launch_bounds__(256) k_asian_sums(const double* __restrict__ arith, const double* __restrict__ geo,
+                                                    uint64_t n, int mode, const double* __restrict__ means,
+                                                    double* __restrict__ partials) {
+  double s0 = 0.0, s1 = 0.0;
+  const double ma = mode ? means[0] : 0.0, mg = mode ? means[1] : 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    if (mode == 0) {
+      s0 += arith[i];
+      s1 += geo[i];
+    } else {
+      const double dg = geo[i] - mg;
+      s0 += (arith[i] - ma) * dg;
+      s1 += dg * dg;
+    }
+  }
+  block_sum2_store(s0, s1, partials + 2 * (uint64_t)blockIdx.x);
+}
+
+// One thread: the means of the mode-0 totals (means[i] = totals[i] / n).
+__global__ void k_asian_means(const double* __restrict__ totals, uint64_t n, double* __restrict__ means) {
+  if (threadIdx.x == 0) {
+    means[0] = totals[0] / (double)n;
+    means[1] = totals[1] / (double)n;
+  }
+}
+
+}  // namespace
+
+int exotic_grid(uint64_t n, int sms) {
+  const uint64_t want = (n + 127) / 128;
+  const uint64_t cap = (uint64_t)sms * 32;
+  return (int)(want < cap ? (want ? want : 1) : cap);
+}
+
+void launch_exotic(const ExoticLaunch& a, int grid, cudaStream_t st) { k_exotic<<<grid, 128, 0, st>>>(a); }
+
+void launch_asian_sums(const double* arith, const double* geo, uint64_t n, int mode, const double* means,
+                       double* partials, int grid, cudaStream_t st) {
+  k_asian_sums<<<grid, 256, 0, st>>>(arith, geo, n, mode, means, partials);
+}
+
+void launch_asian_means(const double* totals, uint64_t n, double* means, cudaStream_t st) {
+  k_asian_means<<<1, 32, 0, st>>>(totals, n, means);
+}
+
+}  // namespace stocha
