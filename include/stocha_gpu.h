@@ -41,6 +41,7 @@ extern "C" {
 #define STOCHA_MODEL_HESTON 1
 #define STOCHA_MODEL_MERTON 2
 #define STOCHA_MODEL_MULTI_GBM 3
+#define STOCHA_MODEL_HULL_WHITE 4 /* r0 in s0, a in kappa, theta, sigma (FP64 paths only) */
 
 #define STOCHA_PAYOFF_CALL 0
 #define STOCHA_PAYOFF_PUT 1
@@ -111,6 +112,10 @@ int stocha_merton_jump_diffusion(stocha_ctx* ctx, double s0, double mu, double s
 /* replaces #[pyfunction] multi_gbm, src/lib.rs:759-827 ->
  * finance/multi_gbm.rs:22 multi_gbm_paths (+ copula/gaussian.rs:76 cholesky).
  * corr is row-major corr_rows x corr_cols. */
+/* hull_white (lib.rs:604-649, finance/hull_white.rs:26-57): short-rate paths
+ * by the exact transition, out[n_paths * (steps+1)] (FP64). */
+int stocha_hull_white(stocha_ctx* ctx, double r0, double a, double theta, double sigma, double t, uint64_t steps,
+                      uint64_t n_paths, uint64_t seed, double* out);
 int stocha_multi_gbm(stocha_ctx* ctx, size_t n_assets, const double* s0, const double* mu, const double* sigma,
                      const double* corr, size_t corr_rows, size_t corr_cols, double t, uint64_t steps,
                      uint64_t n_paths, uint64_t seed, int32_t antithetic, double* out);
@@ -263,6 +268,16 @@ int stocha_lookback_price(stocha_ctx* ctx, double s, double r, double sigma, dou
                           const char* strike_type, const char* option_type, double k, double q, uint64_t n_paths,
                           uint64_t seed, const char* method, double running_max, double running_min,
                           double* price);
+
+/* --------------------------------------------------------------- VaR/CVaR
+ * replaces var_cvar (src/lib.rs:505-520, src/risk/var_cvar.rs:7-43):
+ * out2 = {VaR, CVaR} of the losses -returns at `confidence`.  The returns are
+ * host memory (stocha_var_cvar) or device memory (stocha_var_cvar_device,
+ * e.g. returns computed from device-resident paths).  No sort: a radix
+ * select on total-order keys finds the VaR loss exactly; CVaR is the mean of
+ * the sorted tail. */
+int stocha_var_cvar(stocha_ctx* ctx, const double* returns, uint64_t n, double confidence, double* out2);
+int stocha_var_cvar_device(stocha_ctx* ctx, const double* returns_dev, uint64_t n, double confidence, double* out2);
 
 /* ------------------------------------------------------------- autotuner
  * No counterpart in the reference.  The fused FP32 pricing kernels have a

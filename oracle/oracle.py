@@ -77,6 +77,8 @@ def lib():
         L.oracle_asian_floating_seasoned.restype = _dbl
         L.oracle_lookback_mc.argtypes = [_dbl] * 6 + [_u64, _int, _int, _dbl, _dbl, _u64, _u64, _int]
         L.oracle_lookback_mc.restype = _dbl
+        L.oracle_hull_white.argtypes = [_dbl] * 5 + [_u64, _u64, _u64, _int, _pdbl]
+        L.oracle_var_cvar.argtypes = [_pdbl, _u64, _dbl, _pdbl]
         _lib = L
     return _lib
 
@@ -275,4 +277,19 @@ def lookback_mc(s, r, sigma, t, n_steps=252, strike_type="floating", option_type
     return lib().oracle_lookback_mc(s, k, r, q, sigma, t, n_steps, int(strike_type == "fixed"),
                                     int(option_type == "call"), nan if running_max is None else running_max,
                                     nan if running_min is None else running_min, n_paths, seed, threads)
+
+
+def hull_white(r0, a, theta, sigma, t, steps, n_paths, seed=42, threads=0):
+    """hull_white.rs:26-57 hull_white_paths."""
+    out = np.empty((n_paths, steps + 1), np.float64)
+    lib().oracle_hull_white(r0, a, theta, sigma, t, steps, n_paths, seed, threads, _p(out))
+    return out
+
+
+def var_cvar(returns, confidence):
+    """var_cvar.rs:7-43 (sort by total_cmp, VaR at rank ceil(c n), CVaR = tail mean)."""
+    r = np.ascontiguousarray(returns, np.float64)
+    out = np.zeros(2)
+    lib().oracle_var_cvar(_p(r), r.size, confidence, _p(out))
+    return float(out[0]), float(out[1])
 

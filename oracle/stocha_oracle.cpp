@@ -938,3 +938,45 @@ ORACLE_API double oracle_lookback_mc(double s0, double k, double r, double q, do
   for (double v : pay) total += v;
   return discount * total / (double)n_paths;
 }
+
+// hull_white.rs:26-57: exact-transition short-rate paths, one stream per path
+// with block (steps + 1024) * 4.
+ORACLE_API void oracle_hull_white(double r0, double a, double theta, double sigma, double t, uint64_t steps,
+                                  uint64_t n_paths, uint64_t seed, int threads, double* out) {
+  const double dt = t / (double)steps;
+  const double e = std::exp(-a * dt);
+  const double mean_reversion = (theta / a) * (1.0 - e);
+  const double vol = sigma * std::sqrt((1.0 - e * e) / (2.0 * a));
+  const u128 block = ((u128)steps + 1024) * 4;
+  const uint64_t len = steps + 1;
+  parallel_for(n_paths, threads, [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t i = lo; i < hi; ++i) {
+      Pcg g = path_stream(seed, i, block);
+      double* row = out + i * len;
+      row[0] = r0;
+      for (uint64_t s = 0; s < steps; ++s) {
+        const double z = zig_normal(g);
+        row[s + 1] = row[s] * e + mean_reversion + vol * z;
+      }
+    }
+  });
+}
+
+// var_cvar.rs:7-43: losses = -returns sorted by total_cmp; VaR = losses[idx],
+// idx = min(ceil(confidence * n), n - 1); CVaR = mean of losses[idx..].
+ORACLE_API void oracle_var_cvar(const double* returns, uint64_t n, double confidence, double* out2) {
+  std::vector<double> losses(n);
+  for (uint64_t i = 0; i < n; ++i) losses[i] = -returns[i];
+  auto key = [](double v) {
+    uint64_t b;
+    std::memcpy(&b, &v, 8);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+  };
+  std::sort(losses.begin(), losses.end(), [&](double a, double b) { return key(a) < key(b); });
+  uint64_t idx = (uint64_t)std::ceil(confidence * (double)n);
+  if (idx > n - 1) idx = n - 1;
+  double s = 0.0;
+  for (uint64_t i = idx; i < n; ++i) s += losses[i];
+  out2[0] = losses[idx];
+  out2[1] = s / (double)(n - idx);
+}

@@ -32,12 +32,14 @@ __all__ = [
     "heston",
     "merton_jump_diffusion",
     "multi_gbm",
+    "hull_white",
     "lsmc_american_option",
     "greeks_fd",
     "greeks_pathwise",
     "barrier_price",
     "asian_price",
     "lookback_price",
+    "var_cvar",
     "greeks_batch",
     "price_european",
     "model_struct",
@@ -116,6 +118,13 @@ def multi_gbm(s0: list, mu: list, sigma: list, corr: np.ndarray, t: float, steps
                              t=t, steps=steps, n_paths=n_paths, seed=seed, antithetic=antithetic)
 
 
+def hull_white(r0: float, a: float, theta: float, sigma: float, t: float, steps: int, n_paths: int,
+               seed: int = 42) -> np.ndarray:
+    """Hull-White one-factor short-rate paths by the exact transition, shape ``(n_paths, steps + 1)``
+    (python/stocha/__init__.py hull_white)."""
+    return _stocha.hull_white(r0=r0, a=a, theta=theta, sigma=sigma, t=t, steps=steps, n_paths=n_paths, seed=seed)
+
+
 def lsmc_american_option(s0: float, k: float, r: float, sigma: float, t: float, steps: int, n_paths: int,
                          is_put: bool = True, poly_degree: int = 3, seed: int = 42,
                          precision: str = "fp64") -> tuple[float, float]:
@@ -173,6 +182,13 @@ def lookback_price(s: float, r: float, sigma: float, t: float, n_steps: int = 25
     return _stocha.lookback_price(s, r, sigma, t, n_steps=n_steps, strike_type=strike_type, option_type=option_type,
                                   k=k, q=q, n_paths=n_paths, seed=seed, method=method, running_max=running_max,
                                   running_min=running_min)
+
+
+def var_cvar(returns: np.ndarray, confidence: float) -> tuple[float, float]:
+    """Value-at-Risk and Conditional VaR of a return series (python/stocha/__init__.py var_cvar):
+    losses are -returns; VaR is the loss at rank ceil(confidence * n) of the sorted losses and CVaR
+    the mean of the losses from there on.  Computed on the GPU by a radix select (no sort)."""
+    return _stocha.var_cvar(returns, confidence)
 
 
 # ------------------------------------------------------- GB300 additions ---

@@ -24,7 +24,7 @@ STOCHA_ERR_TIMEOUT = 7
 REQ_PRICE, REQ_GREEKS, REQ_LSMC = 0, 1, 2
 
 FP64, FP32 = 0, 1
-MODEL_GBM, MODEL_HESTON, MODEL_MERTON, MODEL_MULTI_GBM = 0, 1, 2, 3
+MODEL_GBM, MODEL_HESTON, MODEL_MERTON, MODEL_MULTI_GBM, MODEL_HULL_WHITE = 0, 1, 2, 3, 4
 PAYOFF_CALL, PAYOFF_PUT = 0, 1
 
 c_u64 = ctypes.c_uint64
@@ -102,6 +102,7 @@ SIGNATURES = [
     ("stocha_gbm", c_i32, [c_void_p, c_dbl, c_dbl, c_dbl, c_dbl, c_u64, c_u64, c_u64, c_i32, c_dbl, P_dbl]),
     ("stocha_heston", c_i32, [c_void_p] + [c_dbl] * 8 + [c_u64, c_u64, c_u64, c_char_p, P_dbl]),
     ("stocha_merton_jump_diffusion", c_i32, [c_void_p] + [c_dbl] * 7 + [c_u64, c_u64, c_u64, P_dbl]),
+    ("stocha_hull_white", c_i32, [c_void_p] + [c_dbl] * 5 + [c_u64, c_u64, c_u64, P_dbl]),
     ("stocha_multi_gbm", c_i32, [c_void_p, c_size, P_dbl, P_dbl, P_dbl, P_dbl, c_size, c_size, c_dbl, c_u64, c_u64,
                                  c_u64, c_i32, P_dbl]),
     ("stocha_paths_device", c_i32, [c_void_p, ctypes.POINTER(StochaModel), c_u64, c_i32, c_void_p]),
@@ -129,6 +130,8 @@ SIGNATURES = [
                                                                c_u64, c_char_p, c_dbl, c_dbl, P_dbl]),
     ("stocha_lookback_price", c_i32, [c_void_p] + [c_dbl] * 4 + [c_u64, c_char_p, c_char_p, c_dbl, c_dbl, c_u64,
                                                                   c_u64, c_char_p, c_dbl, c_dbl, P_dbl]),
+    ("stocha_var_cvar", c_i32, [c_void_p, P_dbl, c_u64, c_dbl, P_dbl]),
+    ("stocha_var_cvar_device", c_i32, [c_void_p, c_void_p, c_u64, c_dbl, P_dbl]),
     ("stocha_autotune", c_i32, [c_void_p, ctypes.POINTER(StochaModel), c_i32, ctypes.POINTER(StochaTuneResult)]),
     ("stocha_tune_get", c_i32, [c_i32, c_i32, ctypes.POINTER(StochaTuneResult)]),
     ("stocha_tune_set", c_i32, [c_i32, c_i32, c_i32, c_i32, c_i32, c_i32]),

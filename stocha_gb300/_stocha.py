@@ -151,6 +151,17 @@ def merton_jump_diffusion(s0, mu, sigma, lambda_, mu_j, sigma_j, t, steps, n_pat
     return out
 
 
+def hull_white(r0, a, theta, sigma, t, steps, n_paths, seed=42):
+    """lib.rs:604-649: (n_paths, steps + 1) float64 Hull-White short-rate paths
+    by the exact transition; column 0 is r0."""
+    vals = [_f64(v, n) for v, n in zip((r0, a, theta, sigma, t), ("r0", "a", "theta", "sigma", "t"))]
+    steps, n_paths = _usize(steps, "steps"), _usize(n_paths, "n_paths")
+    seed = _usize(seed, "seed")
+    out = _alloc(n_paths, steps + 1, vals[1] > 0 and vals[3] > 0 and vals[4] > 0)
+    check(load().stocha_hull_white(None, *vals, steps, n_paths, seed, dptr(out)))
+    return out
+
+
 def multi_gbm(s0, mu, sigma, corr, t, steps, n_paths, seed=42, antithetic=False):
     """lib.rs:759-827: (n_paths, steps + 1, n_assets) float64 paths."""
     s0 = np.ascontiguousarray([_f64(v, "s0") for v in s0], np.float64)
@@ -344,4 +355,16 @@ def lookback_price(s, r, sigma, t, n_steps=252, strike_type="floating", option_t
                                        seed, method.encode(), _opt_f64(running_max, "running_max"),
                                        _opt_f64(running_min, "running_min"), ctypes.byref(out)))
     return float(out.value)
+
+
+# -------------------------------------------------------------- risk -------
+def var_cvar(returns, confidence):
+    """lib.rs:505-520: (VaR, CVaR) of the losses -returns at `confidence`."""
+    if not isinstance(returns, np.ndarray) or returns.ndim != 1 or returns.dtype != np.float64:
+        raise TypeError("argument 'returns': must be a 1-D float64 numpy.ndarray")
+    confidence = _f64(confidence, "confidence")
+    r = np.ascontiguousarray(returns)
+    out = np.zeros(2, np.float64)
+    check(load().stocha_var_cvar(None, dptr(r) if r.size else None, r.size, confidence, dptr(out)))
+    return float(out[0]), float(out[1])
 

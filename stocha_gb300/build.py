@@ -30,13 +30,14 @@ CUDA_UNITS = {
     "rng.cu": ["--fmad=false"],
     "lsmc.cu": [],
     "exotics.cu": ["--fmad=false"],
+    "risk.cu": [],
     "greeks.cu": [],
     "batch.cu": [],
     "peaks.cu": [],
     "noalloc.cu": [],
 }
 HOST_UNITS = ["api.cpp", "rng_host.cpp", "lsmc_host.cpp", "greeks_host.cpp", "batch_host.cpp", "serve.cpp",
-              "hostcopy.cpp", "exotics_host.cpp"]
+              "hostcopy.cpp", "exotics_host.cpp", "risk_host.cpp"]
 
 
 def _cuda_home() -> str:

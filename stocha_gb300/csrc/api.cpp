@@ -387,6 +387,25 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
       *block = ((u128)m->steps * (u128)na + 1024) * 2;
       return STOCHA_OK;
     }
+    case STOCHA_MODEL_HULL_WHITE: {  // lib.rs:617-636, hull_white.rs:26-45 (r0 in s0, a in kappa)
+      if (check) {
+        if (m->kappa <= 0.0) return set_error(STOCHA_ERR_VALUE, "a must be positive");
+        if (m->sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
+        if (m->t <= 0.0) return set_error(STOCHA_ERR_VALUE, "t must be positive");
+        if (m->steps == 0 || m->n_paths == 0)
+          return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+      }
+      const double dt = m->t / steps_f;
+      const double e = std::exp(-m->kappa * dt);
+      HullWhiteK& H = L->hw;
+      H.r0 = m->s0;
+      H.e = e;
+      H.mean_reversion = (m->theta / m->kappa) * (1.0 - e);
+      H.vol = m->sigma * std::sqrt((1.0 - e * e) / (2.0 * m->kappa));
+      *row_len = m->steps + 1;
+      *block = ((u128)m->steps + 1024) * 4;
+      return STOCHA_OK;
+    }
     default:
       return set_error(STOCHA_ERR_VALUE, "unknown model kind");
   }
@@ -758,6 +777,21 @@ int stocha_merton_jump_diffusion(stocha_ctx* ctx, double s0, double mu, double s
   m.lambda_ = lambda_;
   m.mu_j = mu_j;
   m.sigma_j = sigma_j;
+  m.t = t;
+  m.steps = steps;
+  m.n_paths = n_paths;
+  return paths_to_host(ctx, &m, seed, out);
+}
+
+int stocha_hull_white(stocha_ctx* ctx, double r0, double a, double theta, double sigma, double t, uint64_t steps,
+                      uint64_t n_paths, uint64_t seed, double* out) {
+  stocha_model m;
+  std::memset(&m, 0, sizeof m);
+  m.kind = STOCHA_MODEL_HULL_WHITE;
+  m.s0 = r0;
+  m.kappa = a;
+  m.theta = theta;
+  m.sigma = sigma;
   m.t = t;
   m.steps = steps;
   m.n_paths = n_paths;

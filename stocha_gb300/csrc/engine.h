@@ -10,7 +10,7 @@ namespace stocha {
 
 constexpr int kMaxAssets = 16;
 
-enum Model : int { kGbm = 0, kHeston = 1, kMerton = 2, kMultiGbm = 3 };
+enum Model : int { kGbm = 0, kHeston = 1, kMerton = 2, kMultiGbm = 3, kHullWhite = 4 };
 // In-kernel payoffs of the fused FP64 kernels.  kPw*: the pathwise (IPA)
 // estimators of greeks.rs:387-418 (aux = s0, r, sigma, t).
 enum Payoff : int { kCall = 0, kPut = 1, kPwDeltaCall = 2, kPwDeltaPut = 3, kPwVegaCall = 4, kPwVegaPut = 5 };
@@ -35,6 +35,10 @@ struct MultiK {  // multi_gbm.rs:22-40
   int na;
   double s0[kMaxAssets], drift[kMaxAssets], diffusion[kMaxAssets];
   double L[kMaxAssets * kMaxAssets];  // lower Cholesky factor, row-major
+};
+
+struct HullWhiteK {  // hull_white.rs:26-30: exact transition constants
+  double r0, e, mean_reversion, vol;
 };
 
 // FP32 constants of the FP32 kernels, rounded once on the host: a double
@@ -72,6 +76,7 @@ struct PathLaunch {
   HestonK heston;
   MertonK merton;
   MultiK multi;
+  HullWhiteK hw;
   F32K f32;
 };
 

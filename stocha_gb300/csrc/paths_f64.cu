@@ -257,6 +257,30 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
   if (err) atomicOr(a.err, err);
 }
 
+// Hull-White one-factor short rate by its exact Gaussian transition
+// (hull_white.rs:26-57): r <- r * e + (theta/a)(1 - e) + vol * z; paths only.
+__global__ void __launch_bounds__(128) k_hull_white_f64(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const HullWhiteK& H = a.hw;
+  unsigned err = 0;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+    const uint64_t row = a.row_begin + lrow;
+    PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
+    double x = H.r0;
+    store64(a, lrow, 0, 1, 0, x);
+#pragma unroll 1
+    for (uint64_t k = 1; k <= a.steps; ++k) {
+      const double z = normal_f64(s, c, zs, err);
+      x = x * H.e + H.mean_reversion + H.vol * z;
+      store64(a, lrow, k, 1, 0, x);
+    }
+  }
+  if (err) atomicOr(a.err, err);
+}
+
 __global__ void k_debug_exp(const double* __restrict__ x, double* __restrict__ y, uint64_t n,
                             const ZigTables* tabs) {
   __shared__ ZigShared zs;
@@ -321,6 +345,10 @@ int launch_paths_f64(const PathLaunch& L, cudaStream_t st) {
       break;
     case kMultiGbm:
       if (store) launch_multi<true>(L, G, B, st); else launch_multi<false>(L, G, B, st);
+      break;
+    case kHullWhite:
+      if (!store) return -1;  // rate paths have no in-kernel payoff
+      k_hull_white_f64<<<G, B, 0, st>>>(L);
       break;
     default:
       return -1;

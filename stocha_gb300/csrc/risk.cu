@@ -1,0 +1,98 @@
+// VaR / CVaR of a return series on the device (src/risk/var_cvar.rs:7-43).
+//
+// The reference negates the returns into losses, sorts them with total_cmp
+// and reads the loss at rank idx = min(ceil(confidence * n), n - 1); CVaR is
+// the mean of the sorted tail losses[idx..].  Here nothing is sorted: losses
+// are mapped to 64-bit keys whose unsigned order is total_cmp's order, and an
+// 8-pass radix select (8 bits per pass, histograms in shared memory) finds the
+// key of rank idx, the number of smaller keys and the number of equal keys.
+// The tail is then every loss with a larger key plus the copies of the VaR
+// value that the sorted order places at or after idx.  VaR is exact; CVaR
+// differs from the reference's sequential sum by summation order only.
+#include <cuda_runtime.h>
+
+#include "reduce.cuh"
+#include "risk_kernels.h"
+
+namespace stocha {
+namespace {
+
+// total_cmp order as unsigned order: flip all bits of negatives, the sign bit
+// of the rest.
+__device__ __forceinline__ uint64_t loss_key(double ret) {
+  const uint64_t b = (uint64_t)__double_as_longlong(-ret);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void __launch_bounds__(256) k_check_finite(const double* __restrict__ r, uint64_t n,
+                                                      unsigned* __restrict__ bad) {
+  bool any = false;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    any |= !isfinite(r[i]);
+  if (__syncthreads_or(any) && threadIdx.x == 0) atomicOr(bad, 1u);
+}
+
+// One select pass: histogram of digit `shift` of the keys that carry the
+// prefix found so far.
+__global__ void __launch_bounds__(256) k_select_hist(const double* __restrict__ r, uint64_t n,
+                                                     const SelectState* __restrict__ st, int shift,
+                                                     unsigned long long* __restrict__ hist) {
+  __shared__ unsigned h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const uint64_t prefix = st->prefix, mask = st->mask;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t k = loss_key(r[i]);
+    if ((k & mask) == prefix) atomicAdd(&h[(k >> shift) & 0xFF], 1u);
+  }
+  __syncthreads();
+  if (h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], (unsigned long long)h[threadIdx.x]);
+}
+
+// One thread: the digit holding the wanted rank; clears the histogram.
+__global__ void k_select_step(SelectState* __restrict__ st, int shift, unsigned long long* __restrict__ hist) {
+  if (threadIdx.x != 0) return;
+  uint64_t rank = st->rank, below = 0;
+  int d = 0;
+  for (; d < 255; ++d) {
+    if (rank < below + hist[d]) break;
+    below += hist[d];
+  }
+  st->less += below;
+  st->rank = rank - below;
+  st->equal = hist[d];
+  st->prefix |= (uint64_t)d << shift;
+  st->mask |= (uint64_t)0xFF << shift;
+  for (int j = 0; j < 256; ++j) hist[j] = 0;
+}
+
+// Sum of the losses with keys above the selected one.
+__global__ void __launch_bounds__(256) k_tail_sum(const double* __restrict__ r, uint64_t n,
+                                                  const SelectState* __restrict__ st, double* __restrict__ part) {
+  const uint64_t key = st->prefix;
+  double s = 0.0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    if (loss_key(r[i]) > key) s += -r[i];
+  block_sum2_store(s, 0.0, part + 2 * (uint64_t)blockIdx.x);
+}
+
+}  // namespace
+
+void launch_check_finite(const double* r, uint64_t n, unsigned* bad, int grid, cudaStream_t st) {
+  k_check_finite<<<grid, 256, 0, st>>>(r, n, bad);
+}
+
+void launch_select(const double* r, uint64_t n, SelectState* state, unsigned long long* hist, int grid,
+                   cudaStream_t st) {
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    k_select_hist<<<grid, 256, 0, st>>>(r, n, state, shift, hist);
+    k_select_step<<<1, 32, 0, st>>>(state, shift, hist);
+  }
+}
+
+void launch_tail_sum(const double* r, uint64_t n, const SelectState* state, double* part, int grid,
+                     cudaStream_t st) {
+  k_tail_sum<<<grid, 256, 0, st>>>(r, n, state, part);
+}
+
+}  // namespace stocha

@@ -240,3 +240,35 @@ def test_tune_table_host_logic(stocha):
     finally:
         stocha.tune_set("gbm", before["block"], before["ilp"], before["waves"], variant=before["variant"])
         stocha.tune_set("multi_gbm", 256, 1, 1, variant=0, n_assets=3)
+
+
+def test_hull_white_validation(stocha):
+    """hull_white's argument checks (lib.rs:617-636) happen before any CUDA call."""
+    for kw, msg in [(dict(a=0.0), "a must be positive"), (dict(sigma=0.0), "sigma must be positive"),
+                    (dict(t=0.0), "t must be positive"), (dict(steps=0), "steps and n_paths must be positive"),
+                    (dict(n_paths=0), "steps and n_paths must be positive")]:
+        args = dict(r0=0.05, a=0.1, theta=0.005, sigma=0.01, t=1.0, steps=12, n_paths=10)
+        args.update(kw)
+        with pytest.raises(ValueError, match=msg):
+            stocha.hull_white(**args)
+
+
+def test_var_cvar_validation(stocha):
+    """var_cvar's checks on confidence and emptiness (lib.rs:507-517) come
+    before any CUDA call; non-float64 input is a TypeError as in PyO3."""
+    r = np.array([0.01, -0.02, 0.03])
+    for c in (0.0, 1.0, -0.5, 1.5):
+        with pytest.raises(ValueError, match=r"confidence must be in \(0, 1\)"):
+            stocha.var_cvar(r, c)
+    with pytest.raises(ValueError, match="returns must not be empty"):
+        stocha.var_cvar(np.array([], np.float64), 0.95)
+    with pytest.raises(TypeError):
+        stocha.var_cvar(np.array([1, 2, 3], np.int64), 0.95)
+
+
+def test_oracle_var_cvar_known_values(oracle):
+    """The oracle against the reference's own unit tests (var_cvar.rs:50-75)."""
+    v, c = oracle.var_cvar(np.array([-(i * 0.01) for i in range(1, 11)]), 0.9)
+    assert abs(v - 0.10) < 1e-10 and abs(c - 0.10) < 1e-10
+    v, c = oracle.var_cvar(np.array([i * 0.01 for i in range(1, 21)]), 0.95)
+    assert v < 0 and c <= v + 1e-10
