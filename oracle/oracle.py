@@ -79,6 +79,8 @@ def lib():
         L.oracle_lookback_mc.restype = _dbl
         L.oracle_hull_white.argtypes = [_dbl] * 5 + [_u64, _u64, _u64, _int, _pdbl]
         L.oracle_var_cvar.argtypes = [_pdbl, _u64, _dbl, _pdbl]
+        L.oracle_gaussian_copula.argtypes = [_pdbl, _int, _u64, _u64, _pdbl]
+        L.oracle_gaussian_copula.restype = _int
         _lib = L
     return _lib
 
@@ -292,4 +294,12 @@ def var_cvar(returns, confidence):
     out = np.zeros(2)
     lib().oracle_var_cvar(_p(r), r.size, confidence, _p(out))
     return float(out[0]), float(out[1])
+
+
+def gaussian_copula(corr, n_samples, seed=42):
+    """copula/gaussian.rs:15-73 gaussian_copula_samples."""
+    c = np.ascontiguousarray(corr, np.float64)
+    out = np.empty((n_samples, c.shape[0]))
+    assert lib().oracle_gaussian_copula(_p(c), c.shape[0], n_samples, seed, _p(out)) == 0
+    return out
 

@@ -980,3 +980,37 @@ ORACLE_API void oracle_var_cvar(const double* returns, uint64_t n, double confid
   out2[0] = losses[idx];
   out2[1] = s / (double)(n - idx);
 }
+
+// copula/gaussian.rs:15-73 with dist/normal_cdf.rs:3-22: one sequential
+// stream; sample i takes the next dim normals; x = L z; u = Phi(x).
+ORACLE_API int oracle_gaussian_copula(const double* corr, int dim, uint64_t n, uint64_t seed, double* out) {
+  std::vector<double> l((size_t)dim * dim, 0.0);
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double sum = corr[i * dim + j];
+      for (int k = 0; k < j; ++k) sum -= l[i * dim + k] * l[j * dim + k];
+      if (i == j) {
+        if (sum <= 0.0) return -1;
+        l[i * dim + j] = std::sqrt(sum);
+      } else {
+        l[i * dim + j] = sum / l[j * dim + j];
+      }
+    }
+  Pcg g = Pcg::seeded((u128)seed);
+  std::vector<double> z(dim);
+  const double sqrt_2pi = std::sqrt(2.0 * M_PI);
+  for (uint64_t i = 0; i < n; ++i) {
+    for (int j = 0; j < dim; ++j) z[j] = zig_normal(g);
+    for (int j = 0; j < dim; ++j) {
+      double x = 0.0;
+      for (int k = 0; k <= j; ++k) x += l[j * dim + k] * z[k];
+      const double t = 1.0 / (1.0 + 0.2316419 * std::fabs(x));
+      const double poly =
+          t * (0.319381530 + t * (-0.356563782 + t * (1.781477937 + t * (-1.821255978 + t * 1.330274429))));
+      const double pdf = std::exp(-0.5 * x * x) / sqrt_2pi;
+      const double cdf_pos = 1.0 - pdf * poly;
+      out[i * dim + j] = x >= 0.0 ? cdf_pos : 1.0 - cdf_pos;
+    }
+  }
+  return 0;
+}

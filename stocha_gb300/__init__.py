@@ -40,6 +40,7 @@ __all__ = [
     "asian_price",
     "lookback_price",
     "var_cvar",
+    "gaussian_copula",
     "greeks_batch",
     "price_european",
     "model_struct",
@@ -182,6 +183,12 @@ def lookback_price(s: float, r: float, sigma: float, t: float, n_steps: int = 25
     return _stocha.lookback_price(s, r, sigma, t, n_steps=n_steps, strike_type=strike_type, option_type=option_type,
                                   k=k, q=q, n_paths=n_paths, seed=seed, method=method, running_max=running_max,
                                   running_min=running_min)
+
+
+def gaussian_copula(corr: np.ndarray, n_samples: int, seed: int = 42) -> np.ndarray:
+    """Samples of a Gaussian copula, shape ``(n_samples, dim)`` in (0, 1) (python/stocha/__init__.py
+    gaussian_copula): one sequential stream, normals generated on the GPU by a parallel parse."""
+    return _stocha.gaussian_copula(corr, n_samples, seed=seed)
 
 
 def var_cvar(returns: np.ndarray, confidence: float) -> tuple[float, float]:

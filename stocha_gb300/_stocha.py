@@ -357,6 +357,20 @@ def lookback_price(s, r, sigma, t, n_steps=252, strike_type="floating", option_t
     return float(out.value)
 
 
+# ------------------------------------------------------------ copulas ------
+def gaussian_copula(corr, n_samples, seed=42):
+    """lib.rs:522-549: (n_samples, dim) uniforms of a Gaussian copula."""
+    if not isinstance(corr, np.ndarray) or corr.ndim != 2 or corr.dtype != np.float64:
+        raise TypeError("argument 'corr': must be a 2-D float64 numpy.ndarray")
+    n_samples, seed = _usize(n_samples, "n_samples"), _usize(seed, "seed")
+    c = np.ascontiguousarray(corr)
+    rows, cols = c.shape
+    out = np.empty((n_samples, rows) if rows == cols else (0, 0), np.float64)
+    check(load().stocha_gaussian_copula(None, dptr(c) if c.size else None, rows, cols, n_samples, seed,
+                                        dptr(out) if out.size else None))
+    return out
+
+
 # -------------------------------------------------------------- risk -------
 def var_cvar(returns, confidence):
     """lib.rs:505-520: (VaR, CVaR) of the losses -returns at `confidence`."""

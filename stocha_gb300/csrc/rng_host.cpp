@@ -67,18 +67,18 @@ int fill_raw(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, void* out) {
   return STOCHA_OK;
 }
 
-int fill_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, double loc, double scale, double* out) {
-  int rc = resolve_ctx(&ctx);
-  if (rc) return rc;
-  if (n == 0) return STOCHA_OK;
-  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
-  cudaSetDevice(ctx->device);
+// The next n values (kind 1: standard normal, 2: loc + scale z) of the stream
+// at (state, inc) into ctx->out on the device, by the parallel parse of
+// rng.cu; *final_pos receives the draws consumed.  ctx locked by the caller.
+int normals_to_device(stocha_ctx* ctx, u128 state, u128 inc, uint64_t n, int kind, double loc, double scale,
+                      uint64_t* final_pos_out) {
   const uint32_t C = kRngChunk;
   // expected 1.0296 draws per normal; generous margin, doubled on shortfall
   double need = (double)n * 1.04 + 16.0 * std::sqrt((double)n) + 2.0 * C;
   uint64_t nchunks = (uint64_t)(need / C) + 2;
   StreamSpec ss;
-  make_stream_spec_state(rng_state(r), rng_inc(r), 1, &ss);
+  make_stream_spec_state(state, inc, 1, &ss);
+  int rc;
   for (int attempt = 0; attempt < 8; ++attempt) {
     const size_t off_counts = 0;
     const size_t off_exits = off_counts + nchunks * kRngEntries * 4;
@@ -112,17 +112,61 @@ int fill_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, double loc
     launch_rng_emit(ss, ctx->d_tabs, nchunks, C, entry, cnt, offset, n, kind, loc, scale, (double*)ctx->out.ptr,
                     final_pos, ctx->d_err, ctx->stream);
     STOCHA_CUDA(cudaGetLastError());
-    if ((rc = copy_to_host_populated(ctx->stream, out, ctx->out.ptr, n * 8))) return rc;
     STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, final_pos, 8, cudaMemcpyDeviceToHost, ctx->stream));
     if ((rc = finish_call(ctx))) return rc;
-    uint64_t fp;
-    std::memcpy(&fp, ctx->h_small, 8);
-    u128 s = rng_state(r);
-    pcg_advance(&s, rng_inc(r), fp);
-    set_state(r, s);
+    std::memcpy(final_pos_out, ctx->h_small, 8);
     return STOCHA_OK;
   }
   return set_error(STOCHA_ERR_DEVICE, "normal stream parse did not cover the request");
+}
+
+int fill_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t n, int kind, double loc, double scale, double* out) {
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  if (n == 0) return STOCHA_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  uint64_t fp = 0;
+  if ((rc = normals_to_device(ctx, rng_state(r), rng_inc(r), n, kind, loc, scale, &fp))) return rc;
+  if ((rc = copy_to_host_populated(ctx->stream, out, ctx->out.ptr, n * 8))) return rc;
+  STOCHA_CUDA(cudaStreamSynchronize(ctx->stream));
+  u128 s = rng_state(r);
+  pcg_advance(&s, rng_inc(r), fp);
+  set_state(r, s);
+  return STOCHA_OK;
+}
+
+// gaussian.rs:21-47 checks and gaussian.rs:76-99 Cholesky, with the
+// reference's messages; l receives the factor (dim x dim, row-major).
+int copula_factor(const double* corr, size_t rows, size_t cols, std::vector<double>* l) {
+  const size_t dim = rows;
+  if (cols != dim) return set_error(STOCHA_ERR_VALUE, "correlation matrix must be square");
+  for (size_t i = 0; i < dim; ++i) {
+    if (std::fabs(corr[i * dim + i] - 1.0) > 1e-10)
+      return set_error(STOCHA_ERR_VALUE, "correlation matrix diagonal element [" + std::to_string(i) + "][" +
+                                             std::to_string(i) + "] must be 1.0, got " + rust_f64(corr[i * dim + i]));
+    for (size_t j = i + 1; j < dim; ++j)
+      if (std::fabs(corr[i * dim + j] - corr[j * dim + i]) > 1e-10)
+        return set_error(STOCHA_ERR_VALUE, "correlation matrix is not symmetric: [" + std::to_string(i) + "," +
+                                               std::to_string(j) + "]=" + rust_f64(corr[i * dim + j]) + " vs [" +
+                                               std::to_string(j) + "," + std::to_string(i) +
+                                               "]=" + rust_f64(corr[j * dim + i]));
+  }
+  l->assign(dim * dim, 0.0);
+  for (size_t i = 0; i < dim; ++i)
+    for (size_t j = 0; j <= i; ++j) {
+      double sum = corr[i * dim + j];
+      for (size_t k = 0; k < j; ++k) sum -= (*l)[i * dim + k] * (*l)[j * dim + k];
+      if (i == j) {
+        if (sum <= 0.0)
+          return set_error(STOCHA_ERR_VALUE, "matrix is not positive-definite (diagonal element " +
+                                                 std::to_string(i) + " = " + rust_f64(sum) + ")");
+        (*l)[i * dim + j] = std::sqrt(sum);
+      } else {
+        (*l)[i * dim + j] = sum / (*l)[j * dim + j];
+      }
+    }
+  return STOCHA_OK;
 }
 
 // ---- minimal JSON reader for the state files of pcg64.rs:10-20 ----------
@@ -290,6 +334,36 @@ int stocha_rng_from_state(const char* json, stocha_rng* out) {
     return set_error(STOCHA_ERR_VALUE, "missing field `seed`");
   }
   return set_error(STOCHA_ERR_VALUE, "invalid type: expected struct SeedOnly");
+}
+
+int stocha_gaussian_copula(stocha_ctx* ctx, const double* corr, size_t rows, size_t cols, uint64_t n_samples,
+                           uint64_t seed, double* out) {
+  std::vector<double> l;
+  int rc = copula_factor(corr, rows, cols, &l);  // gaussian.rs:21-51
+  if (rc) return rc;
+  const size_t dim = rows;
+  if (n_samples == 0 || dim == 0) return STOCHA_OK;
+  if ((rc = resolve_ctx(&ctx))) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (n_samples > (SIZE_MAX / 8) / dim) return set_error(STOCHA_ERR_NOMEM, "output size overflows the address space");
+  // one sequential stream Pcg64Dxsm::new(seed): sample i takes normals
+  // i*dim .. i*dim+dim-1 (NormalSampler::sample_into, gaussian.rs:55-60)
+  u128 st, inc;
+  pcg_seed((u128)seed, &st, &inc);
+  uint64_t fp = 0;
+  const uint64_t nz = n_samples * dim;
+  if ((rc = normals_to_device(ctx, st, inc, nz, 1, 0.0, 1.0, &fp))) return rc;
+  if ((rc = ensure_buf(ctx, ctx->aux, nz * 8 + dim * dim * 8 + 256))) return rc;
+  double* u = (double*)ctx->aux.ptr;
+  double* dl = (double*)((char*)ctx->aux.ptr + ((nz * 8 + 255) & ~(size_t)255));
+  if ((rc = begin_call(ctx))) return rc;
+  STOCHA_CUDA(cudaMemcpyAsync(dl, l.data(), dim * dim * 8, cudaMemcpyHostToDevice, ctx->stream));
+  launch_copula_gaussian((const double*)ctx->out.ptr, dl, n_samples, (int)dim, std::sqrt(2.0 * M_PI), u,
+                         ctx->stream);
+  STOCHA_CUDA(cudaGetLastError());
+  if ((rc = copy_to_host_populated(ctx->stream, out, u, nz * 8))) return rc;
+  return finish_call(ctx);  // l outlives the copy (synchronous)
 }
 
 }  // extern "C"

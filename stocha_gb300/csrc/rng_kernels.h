@@ -19,4 +19,10 @@ void launch_rng_emit(const StreamSpec& ss, const ZigTables* tabs, uint64_t nchun
                      const uint32_t* entry, const uint32_t* cnt, const uint64_t* offset, uint64_t n, int kind,
                      double loc, double scale, double* out, uint64_t* final_pos, unsigned* err, cudaStream_t st);
 
+// Gaussian copula rows: u[i, j] = Phi(sum_{k<=j} L[j, k] z[i, k]) with the
+// reference's normal CDF (dist/normal_cdf.rs, A&S 26.2.17); sqrt_2pi is the
+// host's sqrt(2 pi).
+void launch_copula_gaussian(const double* z, const double* L, uint64_t n, int dim, double sqrt_2pi, double* u,
+                            cudaStream_t st);
+
 }  // namespace stocha

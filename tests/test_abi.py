@@ -272,3 +272,18 @@ def test_oracle_var_cvar_known_values(oracle):
     assert abs(v - 0.10) < 1e-10 and abs(c - 0.10) < 1e-10
     v, c = oracle.var_cvar(np.array([i * 0.01 for i in range(1, 21)]), 0.95)
     assert v < 0 and c <= v + 1e-10
+
+
+def test_gaussian_copula_validation(stocha):
+    """gaussian_copula's matrix checks (copula/gaussian.rs:21-47, 76-99) with
+    the reference's messages, before any CUDA call."""
+    with pytest.raises(ValueError, match="correlation matrix must be square"):
+        stocha.gaussian_copula(np.ones((2, 3)), 10)
+    with pytest.raises(ValueError, match=r"diagonal element \[1\]\[1\] must be 1.0, got 0.9"):
+        stocha.gaussian_copula(np.array([[1.0, 0.2], [0.2, 0.9]]), 10)
+    with pytest.raises(ValueError, match=r"not symmetric: \[0,1\]=0.2 vs \[1,0\]=0.3"):
+        stocha.gaussian_copula(np.array([[1.0, 0.2], [0.3, 1.0]]), 10)
+    with pytest.raises(ValueError, match="matrix is not positive-definite"):
+        stocha.gaussian_copula(np.array([[1.0, 1.5], [1.5, 1.0]]), 10)
+    with pytest.raises(TypeError):
+        stocha.gaussian_copula([[1.0, 0.0], [0.0, 1.0]], 10)

@@ -23,3 +23,32 @@ def test_hull_white_reference_expectations(stocha):
     p = stocha.hull_white(0.10, 1.0, 0.05, 0.01, 5.0, 500, 2000, seed=1)
     assert abs(p[:, -1].mean() - 0.05) < 0.005
     assert np.array_equal(p, stocha.hull_white(0.10, 1.0, 0.05, 0.01, 5.0, 500, 2000, seed=1))
+
+
+@pytest.mark.parametrize("dim,n", [(1, 1), (2, 1000), (3, 200_001), (7, 5000)])
+def test_gaussian_copula_matches_oracle(stocha, oracle, dim, n):
+    """One sequential stream: the device's normals (parallel parse) are the
+    reference's bit for bit; the uniforms differ by the exp in the normal CDF
+    at most (1e-15)."""
+    rng = np.random.default_rng(dim)
+    a = rng.standard_normal((dim, dim + 2))
+    cov = a @ a.T
+    d = np.sqrt(np.diag(cov))
+    corr = cov / np.outer(d, d)
+    corr = (corr + corr.T) / 2
+    np.fill_diagonal(corr, 1.0)
+    got = stocha.gaussian_copula(corr, n, seed=5)
+    want = oracle.gaussian_copula(corr, n, seed=5)
+    assert got.shape == (n, dim)
+    assert np.max(np.abs(got - want)) <= 1e-15
+    assert np.all((got > 0) & (got < 1))
+
+
+def test_gaussian_copula_reference_expectations(stocha):
+    corr = np.array([[1.0, 0.8], [0.8, 1.0]])
+    u = stocha.gaussian_copula(corr, 50_000, seed=42)
+    assert u.shape == (50_000, 2) and np.all((u > 0) & (u < 1))
+    # uniform marginals, positive dependence
+    assert abs(u.mean() - 0.5) < 0.01 and np.corrcoef(u.T)[0, 1] > 0.7
+    assert np.array_equal(u, stocha.gaussian_copula(corr, 50_000, seed=42))
+    assert stocha.gaussian_copula(corr, 0).shape == (0, 2)
