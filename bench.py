@@ -25,6 +25,10 @@ One "step" = one pass of all three models.  Path-steps per step = 3 * 2.52e8
           at 2000/s, through stocha_gb300.Server (40 GB budget): p50/p99
           latency overall and for requests of <= 1e5 paths, requests/s, and
           the per-request error of a sample against the FP64 plain form.
+  exotics_mc, rates_copulas_risk  barrier / Asian / lookback Monte Carlo,
+          Hull-White paths, Gaussian and Student-t copulas and VaR/CVaR
+          through the public API (host arrays), each beside the oracle on a
+          bounded sample.
 
 --impl reference runs the C++ oracle (the reference itself is Rust and cannot
 be built here) on all host cores for the same workload, each step a sample of
@@ -383,6 +387,35 @@ def bench_extras(stocha, torch, cores, skip_cpu):
             row["cpu_cores"] = cores
         ex[name] = row
     res["exotics_mc"] = ex
+    # -- Hull-White paths, copulas, VaR / CVaR (host arrays in and out, as the API returns them)
+    rr = {}
+    corr4 = np.full((4, 4), 0.4) + 0.6 * np.eye(4)
+    returns = np.random.default_rng(7).standard_normal(10_000_000) * 0.02
+    cases = [("hull_white_1e5x252", 1e5 * 252, "path-steps/s",
+              lambda: stocha.hull_white(0.05, 0.1, 0.005, 0.01, 1.0, 252, 100_000),
+              lambda: O.hull_white(0.05, 0.1, 0.005, 0.01, 1.0, 252, 100_000, threads=cores), 1e5 * 252),
+             ("gaussian_copula_1e6x4", 1e6, "samples/s", lambda: stocha.gaussian_copula(corr4, 1_000_000),
+              lambda: O.gaussian_copula(corr4, 100_000), 1e5),
+             ("student_t_copula_1e6x4_nu5", 1e6, "samples/s", lambda: stocha.student_t_copula(corr4, 5.0, 1_000_000),
+              lambda: O.student_t_copula(corr4, 5.0, 100_000), 1e5),
+             ("var_cvar_1e7_returns", 1e7, "returns/s", lambda: stocha.var_cvar(returns, 0.99),
+              lambda: O.var_cvar(returns[:1_000_000], 0.99), 1e6)]
+    for name, units, unit, gpu, cpu, cpu_units in cases:
+        gpu()
+        t0 = time.perf_counter()
+        for _ in range(3):
+            gpu()
+        dt = (time.perf_counter() - t0) / 3
+        row = {"e2e_value": units / dt, "unit": unit, "ms": dt * 1e3}
+        if not skip_cpu:
+            t0 = time.perf_counter()
+            cpu()
+            row["cpu_value"] = cpu_units / (time.perf_counter() - t0)
+            # Hull-White paths are per-path parallel (Rayon in the reference); the
+            # copulas are one sequential stream and VaR one sort, single-threaded there
+            row["cpu_cores"] = cores if name.startswith("hull_white") else 1
+        rr[name] = row
+    res["rates_copulas_risk"] = rr
     # -- config 5: the serving loop
     res["config5_serving"] = bench_serving(stocha)
     return res

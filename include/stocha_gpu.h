@@ -109,18 +109,24 @@ int stocha_merton_jump_diffusion(stocha_ctx* ctx, double s0, double mu, double s
                                  double sigma_j, double t, uint64_t steps, uint64_t n_paths, uint64_t seed,
                                  double* out);
 
-/* replaces #[pyfunction] multi_gbm, src/lib.rs:759-827 ->
- * finance/multi_gbm.rs:22 multi_gbm_paths (+ copula/gaussian.rs:76 cholesky).
- * corr is row-major corr_rows x corr_cols. */
 /* gaussian_copula (lib.rs:522-549, copula/gaussian.rs:15-99): n_samples x dim
  * uniforms from ONE sequential stream Pcg64Dxsm::new(seed) (normals drawn by
  * the parallel stream parse, bit-exact), out[n_samples * dim]. */
 int stocha_gaussian_copula(stocha_ctx* ctx, const double* corr, size_t rows, size_t cols, uint64_t n_samples,
                            uint64_t seed, double* out);
+/* student_t_copula (lib.rs:551-578, copula/student_t.rs:93-170): n_samples x dim
+ * uniforms from ONE sequential stream; a sample's chi-square (Marsaglia-Tsang
+ * gamma) and normals are found by a speculative parallel parse of the stream
+ * (exact consumption), out[n_samples * dim]. */
+int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, size_t cols, double nu,
+                            uint64_t n_samples, uint64_t seed, double* out);
 /* hull_white (lib.rs:604-649, finance/hull_white.rs:26-57): short-rate paths
  * by the exact transition, out[n_paths * (steps+1)] (FP64). */
 int stocha_hull_white(stocha_ctx* ctx, double r0, double a, double theta, double sigma, double t, uint64_t steps,
                       uint64_t n_paths, uint64_t seed, double* out);
+/* replaces #[pyfunction] multi_gbm, src/lib.rs:759-827 ->
+ * finance/multi_gbm.rs:22 multi_gbm_paths (+ copula/gaussian.rs:76 cholesky).
+ * corr is row-major corr_rows x corr_cols. */
 int stocha_multi_gbm(stocha_ctx* ctx, size_t n_assets, const double* s0, const double* mu, const double* sigma,
                      const double* corr, size_t corr_rows, size_t corr_cols, double t, uint64_t steps,
                      uint64_t n_paths, uint64_t seed, int32_t antithetic, double* out);

@@ -81,6 +81,10 @@ def lib():
         L.oracle_var_cvar.argtypes = [_pdbl, _u64, _dbl, _pdbl]
         L.oracle_gaussian_copula.argtypes = [_pdbl, _int, _u64, _u64, _pdbl]
         L.oracle_gaussian_copula.restype = _int
+        L.oracle_student_t_copula.argtypes = [_pdbl, _int, _dbl, _u64, _u64, _pdbl]
+        L.oracle_student_t_copula.restype = _int
+        L.oracle_student_t_cdf.argtypes = [_dbl, _dbl]
+        L.oracle_student_t_cdf.restype = _dbl
         _lib = L
     return _lib
 
@@ -302,4 +306,17 @@ def gaussian_copula(corr, n_samples, seed=42):
     out = np.empty((n_samples, c.shape[0]))
     assert lib().oracle_gaussian_copula(_p(c), c.shape[0], n_samples, seed, _p(out)) == 0
     return out
+
+
+def student_t_copula(corr, nu, n_samples, seed=42):
+    """copula/student_t.rs:135-170 student_t_copula_samples."""
+    c = np.ascontiguousarray(corr, np.float64)
+    out = np.empty((n_samples, c.shape[0]))
+    assert lib().oracle_student_t_copula(_p(c), c.shape[0], nu, n_samples, seed, _p(out)) == 0
+    return out
+
+
+def student_t_cdf(x, nu):
+    """copula/student_t.rs:8-16 (incomplete beta by modified Lentz, Lanczos log-gamma)."""
+    return lib().oracle_student_t_cdf(float(x), float(nu))
 

@@ -1014,3 +1014,104 @@ ORACLE_API int oracle_gaussian_copula(const double* corr, int dim, uint64_t n, u
   }
   return 0;
 }
+
+// copula/student_t.rs:6-170: one sequential stream; per sample chi-square(nu)
+// by Marsaglia-Tsang gamma, then dim normals; u = T_nu((L z)_j sqrt(nu/chi2)).
+namespace {
+
+double st_lgamma(double x) {  // student_t.rs:74-91 (Lanczos g = 7)
+  static const double C[9] = {0.99999999999980993,  676.5203681218851,     -1259.1392167224028,
+                              771.32342877765313,   -176.61502916214059,   12.507343278686905,
+                              -0.13857109526572012, 9.9843695780195716e-6, 1.5056327351493116e-7};
+  if (x < 0.5) return std::log(M_PI) - std::log(std::sin(M_PI * x)) - st_lgamma(1.0 - x);
+  x -= 1.0;
+  double acc = C[0];
+  for (int i = 1; i < 9; ++i) acc += C[i] / (x + (double)i);
+  const double t = x + 7.0 + 0.5;
+  return 0.5 * std::log(2.0 * M_PI) + (x + 0.5) * std::log(t) - t + std::log(acc);
+}
+
+double st_beta_cf(double x, double a, double b) {  // student_t.rs:33-72
+  const double EPS = 3e-7, FPMIN = 1e-30;
+  const double qab = a + b, qap = a + 1.0, qam = a - 1.0;
+  double c = 1.0, d = std::max(1.0 - qab * x / qap, FPMIN);
+  d = 1.0 / d;
+  double h = d;
+  for (int m = 1; m <= 200; ++m) {
+    const double mf = m, m2 = 2.0 * mf;
+    double aa = mf * (b - mf) * x / ((qam + m2) * (a + m2));
+    d = std::max(std::fabs(1.0 + aa * d), FPMIN);
+    c = std::max(std::fabs(1.0 + aa / c), FPMIN);
+    d = 1.0 / d;
+    h *= d * c;
+    aa = -(a + mf) * (qab + mf) * x / ((a + m2) * (qap + m2));
+    d = std::max(std::fabs(1.0 + aa * d), FPMIN);
+    c = std::max(std::fabs(1.0 + aa / c), FPMIN);
+    d = 1.0 / d;
+    const double del = d * c;
+    h *= del;
+    if (std::fabs(del - 1.0) < EPS) break;
+  }
+  return h;
+}
+
+double st_ibeta(double x, double a, double b) {  // student_t.rs:19-31
+  if (x <= 0.0) return 0.0;
+  if (x >= 1.0) return 1.0;
+  if (x > (a + 1.0) / (a + b + 2.0)) return 1.0 - st_ibeta(1.0 - x, b, a);
+  const double lb = st_lgamma(a) + st_lgamma(b) - st_lgamma(a + b);
+  const double front = std::exp(a * std::log(x) + b * std::log(1.0 - x) - lb) / a;
+  return front * st_beta_cf(x, a, b);
+}
+
+double st_gamma(Pcg& g, double shape) {  // student_t.rs:93-119
+  const double d = shape - 1.0 / 3.0;
+  const double c = 1.0 / std::sqrt(9.0 * d);
+  for (;;) {
+    const double x = zig_normal(g);
+    const double v_inner = 1.0 + c * x;
+    if (v_inner <= 0.0) continue;
+    const double v = v_inner * v_inner * v_inner;
+    const double u = g.next_f64();
+    if (u < 1.0 - 0.0331 * (x * x) * (x * x)) return d * v;
+    if (std::log(u) < 0.5 * x * x + d * (1.0 - v + std::log(v))) return d * v;
+  }
+}
+
+}  // namespace
+
+ORACLE_API int oracle_student_t_copula(const double* corr, int dim, double nu, uint64_t n, uint64_t seed,
+                                       double* out) {
+  std::vector<double> l((size_t)dim * dim, 0.0);
+  for (int i = 0; i < dim; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double sum = corr[i * dim + j];
+      for (int k = 0; k < j; ++k) sum -= l[i * dim + k] * l[j * dim + k];
+      if (i == j) {
+        if (sum <= 0.0) return -1;
+        l[i * dim + j] = std::sqrt(sum);
+      } else {
+        l[i * dim + j] = sum / l[j * dim + j];
+      }
+    }
+  Pcg g = Pcg::seeded((u128)seed);
+  std::vector<double> z(dim);
+  for (uint64_t i = 0; i < n; ++i) {
+    const double chi = 2.0 * st_gamma(g, nu / 2.0);
+    const double scale = std::sqrt(nu / chi);
+    for (int j = 0; j < dim; ++j) z[j] = zig_normal(g);
+    for (int j = 0; j < dim; ++j) {
+      double x = 0.0;
+      for (int k = 0; k <= j; ++k) x += l[j * dim + k] * z[k];
+      const double xs = x * scale;
+      const double ib = st_ibeta(nu / (nu + xs * xs), nu / 2.0, 0.5);
+      out[i * dim + j] = xs >= 0.0 ? 1.0 - 0.5 * ib : 0.5 * ib;
+    }
+  }
+  return 0;
+}
+
+ORACLE_API double oracle_student_t_cdf(double x, double nu) {  // student_t.rs:8-16
+  const double ib = st_ibeta(nu / (nu + x * x), nu / 2.0, 0.5);
+  return x >= 0.0 ? 1.0 - 0.5 * ib : 0.5 * ib;
+}

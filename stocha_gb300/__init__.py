@@ -41,6 +41,7 @@ __all__ = [
     "lookback_price",
     "var_cvar",
     "gaussian_copula",
+    "student_t_copula",
     "greeks_batch",
     "price_european",
     "model_struct",
@@ -189,6 +190,12 @@ def gaussian_copula(corr: np.ndarray, n_samples: int, seed: int = 42) -> np.ndar
     """Samples of a Gaussian copula, shape ``(n_samples, dim)`` in (0, 1) (python/stocha/__init__.py
     gaussian_copula): one sequential stream, normals generated on the GPU by a parallel parse."""
     return _stocha.gaussian_copula(corr, n_samples, seed=seed)
+
+
+def student_t_copula(corr: np.ndarray, nu: float, n_samples: int, seed: int = 42) -> np.ndarray:
+    """Samples of a Student-t copula, shape ``(n_samples, dim)`` in (0, 1) (python/stocha/__init__.py
+    student_t_copula): one sequential stream, parsed in parallel on the GPU."""
+    return _stocha.student_t_copula(corr, nu, n_samples, seed=seed)
 
 
 def var_cvar(returns: np.ndarray, confidence: float) -> tuple[float, float]:

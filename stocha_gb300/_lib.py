@@ -103,6 +103,7 @@ SIGNATURES = [
     ("stocha_heston", c_i32, [c_void_p] + [c_dbl] * 8 + [c_u64, c_u64, c_u64, c_char_p, P_dbl]),
     ("stocha_merton_jump_diffusion", c_i32, [c_void_p] + [c_dbl] * 7 + [c_u64, c_u64, c_u64, P_dbl]),
     ("stocha_gaussian_copula", c_i32, [c_void_p, P_dbl, c_size, c_size, c_u64, c_u64, P_dbl]),
+    ("stocha_student_t_copula", c_i32, [c_void_p, P_dbl, c_size, c_size, c_dbl, c_u64, c_u64, P_dbl]),
     ("stocha_hull_white", c_i32, [c_void_p] + [c_dbl] * 5 + [c_u64, c_u64, c_u64, P_dbl]),
     ("stocha_multi_gbm", c_i32, [c_void_p, c_size, P_dbl, P_dbl, P_dbl, P_dbl, c_size, c_size, c_dbl, c_u64, c_u64,
                                  c_u64, c_i32, P_dbl]),

@@ -371,6 +371,20 @@ def gaussian_copula(corr, n_samples, seed=42):
     return out
 
 
+def student_t_copula(corr, nu, n_samples, seed=42):
+    """lib.rs:551-578: (n_samples, dim) uniforms of a Student-t copula."""
+    if not isinstance(corr, np.ndarray) or corr.ndim != 2 or corr.dtype != np.float64:
+        raise TypeError("argument 'corr': must be a 2-D float64 numpy.ndarray")
+    nu = _f64(nu, "nu")
+    n_samples, seed = _usize(n_samples, "n_samples"), _usize(seed, "seed")
+    c = np.ascontiguousarray(corr)
+    rows, cols = c.shape
+    out = np.empty((n_samples, rows) if rows == cols and not nu <= 2.0 else (0, 0), np.float64)
+    check(load().stocha_student_t_copula(None, dptr(c) if c.size else None, rows, cols, nu, n_samples, seed,
+                                         dptr(out) if out.size else None))
+    return out
+
+
 # -------------------------------------------------------------- risk -------
 def var_cvar(returns, confidence):
     """lib.rs:505-520: (VaR, CVaR) of the losses -returns at `confidence`."""

@@ -31,6 +31,7 @@ CUDA_UNITS = {
     "lsmc.cu": [],
     "exotics.cu": ["--fmad=false"],
     "risk.cu": [],
+    "copula_t.cu": ["--fmad=false"],
     "greeks.cu": [],
     "batch.cu": [],
     "peaks.cu": [],

@@ -1,0 +1,251 @@
+// Student-t copula (src/copula/student_t.rs:93-170) from ONE sequential
+// stream, Pcg64Dxsm::new(seed), in parallel.
+//
+// A sample consumes a variable number of draws: chi-square(nu) by
+// Marsaglia-Tsang's gamma sampler (student_t.rs:93-124: normal, cube,
+// uniform, squeeze or log test, repeat on rejection), then `dim` normals.
+// Its consumption depends only on the draws, so the stream is cut into
+// chunks of C draws and each chunk is parsed from E candidate entry offsets
+// at once (k_tparse: samples starting in the chunk, and where the last one
+// ends).  One thread then chains the true entries chunk by chunk (k_tstitch;
+// a chunk whose entry lies beyond the candidates is parsed there, in order),
+// k_temit re-parses every chunk from its true entry and stores each sample's
+// chi-square and normals, and k_tcdf forms the uniforms
+// u = T_nu((L z)_j * sqrt(nu / chi2)) with the reference's Student-t CDF
+// (regularized incomplete beta by the modified-Lentz continued fraction,
+// Lanczos log-gamma; student_t.rs:6-91).  Every decision uses the
+// reference's FP64 values (exact normals; ln in the gamma test and the CDF
+// from the device libm).
+#include <cuda_runtime.h>
+
+#include "copula_t_kernels.h"
+#include "mc_device.cuh"
+
+namespace stocha {
+namespace {
+
+__device__ __forceinline__ double next_f64(CountingGen& g) { return u64_to_unit_f64(g.next()); }  // pcg64.rs:37-39
+
+// student_t.rs:93-119 (shape >= 1: nu > 2 is enforced)
+__device__ double sample_gamma(CountingGen& g, double d, double c, const SamplerCtx& sc, const ZigShared& zs,
+                               unsigned& err) {
+#pragma unroll 1
+  for (int it = 0; it < 1 << 20; ++it) {
+    const double x = normal_f64(g, sc, zs, err);
+    const double v_inner = 1.0 + c * x;
+    if (v_inner <= 0.0) continue;
+    const double v = v_inner * v_inner * v_inner;
+    const double u = next_f64(g);
+    if (u < 1.0 - 0.0331 * (x * x) * (x * x)) return d * v;
+    if (log(u) < 0.5 * x * x + d * (1.0 - v + log(v))) return d * v;
+  }
+  err |= kErrZigAttempts;
+  return d;
+}
+
+// One sample: chi-square (2 * gamma(nu / 2), student_t.rs:121-124) and dim
+// normals (z may be null: consumption only).
+__device__ __forceinline__ double sample_one(CountingGen& g, const TParse& a, const SamplerCtx& sc,
+                                             const ZigShared& zs, unsigned& err, double* z) {
+  const double chi = 2.0 * sample_gamma(g, a.d, a.c, sc, zs, err);
+  for (int j = 0; j < a.dim; ++j) {
+    const double v = normal_f64(g, sc, zs, err);
+    if (z) z[j] = v;
+  }
+  return chi;
+}
+
+__device__ __forceinline__ CountingGen gen_at(const TParse& a, uint64_t pos) {
+  return CountingGen{pcg_path_state(a.ss, pos), a.ss.inc_lo, a.ss.inc_hi, pos};
+}
+
+// Parses the samples that start in [lo, hi) from a sample start at pos;
+// returns the end of the last one and counts them.
+__device__ uint64_t parse_span(const TParse& a, uint64_t pos, uint64_t hi, const SamplerCtx& sc, const ZigShared& zs,
+                               unsigned& err, uint32_t* count) {
+  CountingGen g = gen_at(a, pos);
+  uint32_t n = 0;
+  while (g.pos < hi) {
+    sample_one(g, a, sc, zs, err, nullptr);
+    ++n;
+  }
+  *count = n;
+  return g.pos;
+}
+
+__global__ void __launch_bounds__(128) k_tparse(const __grid_constant__ TParse a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx sc{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  const uint64_t total = a.nchunks * (uint64_t)a.E;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t chunk = t / a.E, e = t - chunk * a.E;
+    const uint64_t lo = chunk * a.C, hi = lo + a.C;
+    uint32_t cnt = 0;
+    const uint64_t end = parse_span(a, lo + e, hi, sc, zs, err, &cnt);
+    a.exits[t] = end - hi;
+    a.counts[t] = cnt;
+  }
+  if (err) atomicOr(a.err, err);
+}
+
+// One thread: true entry of every chunk and the index of its first sample,
+// until n samples are covered.
+__global__ void k_tstitch(const __grid_constant__ TParse a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  if (threadIdx.x != 0) return;
+  const SamplerCtx sc{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  uint64_t entry = 0, base = 0, used = 0;
+  for (uint64_t c = 0; c < a.nchunks && base < a.n; ++c) {
+    a.entry[c] = entry;
+    a.first[c] = base;
+    uint64_t exit;
+    uint32_t cnt;
+    if (entry >= a.C) {  // a sample spans this whole chunk
+      cnt = 0;
+      exit = entry - a.C;
+    } else if (entry < (uint64_t)a.E) {
+      exit = a.exits[c * a.E + entry];
+      cnt = a.counts[c * a.E + entry];
+    } else {  // beyond the candidates: parse here
+      const uint64_t lo = c * a.C;
+      exit = parse_span(a, lo + entry, lo + a.C, sc, zs, err, &cnt) - (lo + a.C);
+    }
+    base += cnt;
+    entry = exit;
+    used = c + 1;
+  }
+  a.status[0] = used;
+  a.status[1] = base;
+  if (err) atomicOr(a.err, err);
+}
+
+// One thread per chunk: the chunk's samples from its true entry.
+__global__ void __launch_bounds__(128) k_temit(const __grid_constant__ TParse a, const uint64_t* __restrict__ status) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx sc{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  const uint64_t used = status[0];
+  for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < used; c += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t lo = c * a.C, hi = lo + a.C;
+    CountingGen g = gen_at(a, lo + a.entry[c]);
+    uint64_t s = a.first[c];
+    while (g.pos < hi && s < a.n) {
+      double* row = a.raw + s * (uint64_t)(a.dim + 1);
+      row[0] = sample_one(g, a, sc, zs, err, row + 1);
+      ++s;
+    }
+  }
+  if (err) atomicOr(a.err, err);
+}
+
+// ---- Student-t CDF (student_t.rs:6-91) ----
+__device__ double lgamma_lanczos(double x) {  // Lanczos, g = 7, nine coefficients
+  const double C[9] = {0.99999999999980993,  676.5203681218851,     -1259.1392167224028,
+                       771.32342877765313,   -176.61502916214059,   12.507343278686905,
+                       -0.13857109526572012, 9.9843695780195716e-6, 1.5056327351493116e-7};
+  const double PI = 3.14159265358979323846;
+  double refl = 0.0;
+  if (x < 0.5) {  // reflection, at most once for the arguments used here
+    refl = log(PI) - log(sin(PI * x));
+    x = 1.0 - x;
+    x -= 1.0;
+    double acc = C[0];
+    for (int i = 1; i < 9; ++i) acc += C[i] / (x + (double)i);
+    const double t = x + 7.0 + 0.5;
+    return refl - (0.5 * log(2.0 * PI) + (x + 0.5) * log(t) - t + log(acc));
+  }
+  x -= 1.0;
+  double acc = C[0];
+  for (int i = 1; i < 9; ++i) acc += C[i] / (x + (double)i);
+  const double t = x + 7.0 + 0.5;
+  return 0.5 * log(2.0 * PI) + (x + 0.5) * log(t) - t + log(acc);
+}
+
+__device__ double beta_cf(double x, double a, double b) {  // modified Lentz, student_t.rs:40-72
+  const double EPS = 3e-7, FPMIN = 1e-30;
+  const double qab = a + b, qap = a + 1.0, qam = a - 1.0;
+  double c = 1.0;
+  double d = fmax(1.0 - qab * x / qap, FPMIN);
+  d = 1.0 / d;
+  double h = d;
+  for (int m = 1; m <= 200; ++m) {
+    const double mf = (double)m, m2 = 2.0 * mf;
+    double aa = mf * (b - mf) * x / ((qam + m2) * (a + m2));
+    d = fmax(fabs(1.0 + aa * d), FPMIN);
+    c = fmax(fabs(1.0 + aa / c), FPMIN);
+    d = 1.0 / d;
+    h *= d * c;
+    aa = -(a + mf) * (qab + mf) * x / ((a + m2) * (qap + m2));
+    d = fmax(fabs(1.0 + aa * d), FPMIN);
+    c = fmax(fabs(1.0 + aa / c), FPMIN);
+    d = 1.0 / d;
+    const double del = d * c;
+    h *= del;
+    if (fabs(del - 1.0) < EPS) break;
+  }
+  return h;
+}
+
+__device__ double ibeta(double x, double a, double b) {  // student_t.rs:19-31
+  if (x <= 0.0) return 0.0;
+  if (x >= 1.0) return 1.0;
+  bool flip = false;
+  if (x > (a + 1.0) / (a + b + 2.0)) {
+    flip = true;
+    x = 1.0 - x;
+    const double t = a;
+    a = b;
+    b = t;
+  }
+  const double log_beta = lgamma_lanczos(a) + lgamma_lanczos(b) - lgamma_lanczos(a + b);
+  const double front = exp(a * log(x) + b * log(1.0 - x) - log_beta) / a;
+  const double v = front * beta_cf(x, a, b);
+  return flip ? 1.0 - v : v;
+}
+
+__global__ void __launch_bounds__(256) k_tcdf(const double* __restrict__ raw, const double* __restrict__ L,
+                                              uint64_t n, int dim, double nu, double* __restrict__ u) {
+  const uint64_t total = n * (uint64_t)dim;
+  for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t i = e / (uint64_t)dim;
+    const int j = (int)(e - i * (uint64_t)dim);
+    const double* row = raw + i * (uint64_t)(dim + 1);
+    const double scale = sqrt(nu / row[0]);  // student_t.rs:157
+    double x = 0.0;
+    for (int k = 0; k <= j; ++k) x += L[j * dim + k] * row[1 + k];
+    const double xs = x * scale;
+    const double z = nu / (nu + xs * xs);
+    const double ib = ibeta(z, nu / 2.0, 0.5);
+    u[e] = xs >= 0.0 ? 1.0 - 0.5 * ib : 0.5 * ib;
+  }
+}
+
+}  // namespace
+
+void launch_tparse(const TParse& a, cudaStream_t st) {
+  const uint64_t total = a.nchunks * (uint64_t)a.E;
+  uint64_t g = (total + 127) / 128;
+  if (g > 152ull * 64) g = 152ull * 64;
+  k_tparse<<<(unsigned)(g ? g : 1), 128, 0, st>>>(a);
+}
+
+void launch_tstitch(const TParse& a, cudaStream_t st) { k_tstitch<<<1, 32, 0, st>>>(a); }
+
+void launch_temit(const TParse& a, const uint64_t* status, cudaStream_t st) {
+  uint64_t g = (a.nchunks + 127) / 128;
+  k_temit<<<(unsigned)(g ? g : 1), 128, 0, st>>>(a, status);
+}
+
+void launch_tcdf(const double* raw, const double* L, uint64_t n, int dim, double nu, double* u, cudaStream_t st) {
+  const uint64_t total = n * (uint64_t)dim;
+  uint64_t g = (total + 255) / 256;
+  if (g > 152ull * 32) g = 152ull * 32;
+  k_tcdf<<<(unsigned)(g ? g : 1), 256, 0, st>>>(raw, L, n, dim, nu, u);
+}
+
+}  // namespace stocha

@@ -1,0 +1,33 @@
+// Student-t copula kernels (copula_t.cu), used by rng_host.cpp.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "mc_types.h"
+
+namespace stocha {
+
+struct TParse {
+  StreamSpec ss;  // the sequential stream, jump table by draw index
+  const ZigTables* tabs;
+  unsigned* err;
+  uint64_t nchunks, n;  // chunks parsed; samples wanted
+  uint32_t C;           // draws per chunk
+  int E;                // candidate entry offsets per chunk
+  int dim;
+  int pad;
+  double d, c;          // Marsaglia-Tsang constants of shape nu / 2
+  uint64_t* exits;      // nchunks * E: end of the last sample minus the chunk end
+  uint32_t* counts;     // nchunks * E: samples starting in the chunk
+  uint64_t* entry;      // nchunks: true entry offset
+  uint64_t* first;      // nchunks: index of the chunk's first sample
+  uint64_t* status;     // [0] chunks used, [1] samples covered
+  double* raw;          // n * (dim + 1): chi-square, then the dim normals
+};
+
+void launch_tparse(const TParse& a, cudaStream_t st);
+void launch_tstitch(const TParse& a, cudaStream_t st);
+void launch_temit(const TParse& a, const uint64_t* status, cudaStream_t st);
+void launch_tcdf(const double* raw, const double* L, uint64_t n, int dim, double nu, double* u, cudaStream_t st);
+
+}  // namespace stocha

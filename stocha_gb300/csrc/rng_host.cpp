@@ -6,6 +6,7 @@
 #include <vector>
 
 #include "host_common.h"
+#include "copula_t_kernels.h"
 #include "rng_kernels.h"
 
 using namespace stocha;
@@ -364,6 +365,97 @@ int stocha_gaussian_copula(stocha_ctx* ctx, const double* corr, size_t rows, siz
   STOCHA_CUDA(cudaGetLastError());
   if ((rc = copy_to_host_populated(ctx->stream, out, u, nz * 8))) return rc;
   return finish_call(ctx);  // l outlives the copy (synchronous)
+}
+
+int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, size_t cols, double nu,
+                            uint64_t n_samples, uint64_t seed, double* out) {
+  if (nu <= 2.0) return set_error(STOCHA_ERR_VALUE, "nu must be > 2");  // lib.rs:570-572 (NaN passes, as there)
+  std::vector<double> l;
+  if (cols != rows) return set_error(STOCHA_ERR_VALUE, "correlation matrix must be square");  // student_t.rs:146-148
+  // student_t.rs:149 factors the matrix without the diagonal / symmetry checks
+  {
+    const size_t dim = rows;
+    l.assign(dim * dim, 0.0);
+    for (size_t i = 0; i < dim; ++i)
+      for (size_t j = 0; j <= i; ++j) {
+        double sum = corr[i * dim + j];
+        for (size_t k = 0; k < j; ++k) sum -= l[i * dim + k] * l[j * dim + k];
+        if (i == j) {
+          if (sum <= 0.0)
+            return set_error(STOCHA_ERR_VALUE, "matrix is not positive-definite (diagonal element " +
+                                                   std::to_string(i) + " = " + rust_f64(sum) + ")");
+          l[i * dim + j] = std::sqrt(sum);
+        } else {
+          l[i * dim + j] = sum / l[j * dim + j];
+        }
+      }
+  }
+  const size_t dim = rows;
+  if (n_samples == 0 || dim == 0) return STOCHA_OK;
+  int rc;
+  if ((rc = resolve_ctx(&ctx))) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  cudaSetDevice(ctx->device);
+  if (n_samples > (SIZE_MAX / 8) / (dim + 1)) return set_error(STOCHA_ERR_NOMEM, "output size overflows the address space");
+  u128 st, inc;
+  pcg_seed((u128)seed, &st, &inc);
+  TParse a;
+  std::memset(&a, 0, sizeof a);
+  make_stream_spec_state(st, inc, 1, &a.ss);
+  a.tabs = ctx->d_tabs;
+  a.err = ctx->d_err;
+  a.n = n_samples;
+  a.C = 1024;
+  a.dim = (int)dim;
+  a.E = (int)std::min<size_t>(2 * dim + 16, a.C);
+  const double shape = nu / 2.0;  // student_t.rs:121-124, 102-103
+  a.d = shape - 1.0 / 3.0;
+  a.c = 1.0 / std::sqrt(9.0 * a.d);
+  // ~2.1 draws for the chi-square and 1.03 per normal
+  double need = (double)n_samples * (2.3 + 1.06 * (double)dim) + 8.0 * a.C;
+  a.nchunks = (uint64_t)(need / a.C) + 2;
+  for (int attempt = 0; attempt < 8; ++attempt) {
+    const uint64_t nc = a.nchunks;
+    const size_t o_exits = 0;
+    const size_t o_counts = o_exits + nc * a.E * 8;
+    const size_t o_entry = (o_counts + nc * a.E * 4 + 7) & ~(size_t)7;
+    const size_t o_first = o_entry + nc * 8;
+    const size_t o_status = o_first + nc * 8;
+    const size_t o_raw = (o_status + 64 + 255) & ~(size_t)255;
+    const size_t o_l = (o_raw + n_samples * (dim + 1) * 8 + 255) & ~(size_t)255;
+    const size_t o_u = (o_l + dim * dim * 8 + 255) & ~(size_t)255;
+    const size_t bytes = o_u + n_samples * dim * 8;
+    if ((rc = ensure_buf(ctx, ctx->aux, bytes))) return rc;
+    char* base = (char*)ctx->aux.ptr;
+    a.exits = (uint64_t*)(base + o_exits);
+    a.counts = (uint32_t*)(base + o_counts);
+    a.entry = (uint64_t*)(base + o_entry);
+    a.first = (uint64_t*)(base + o_first);
+    a.status = (uint64_t*)(base + o_status);
+    a.raw = (double*)(base + o_raw);
+    double* dl = (double*)(base + o_l);
+    double* u = (double*)(base + o_u);
+    if ((rc = begin_call(ctx))) return rc;
+    launch_tparse(a, ctx->stream);
+    launch_tstitch(a, ctx->stream);
+    STOCHA_CUDA(cudaGetLastError());
+    STOCHA_CUDA(cudaMemcpyAsync(ctx->h_small, a.status, 16, cudaMemcpyDeviceToHost, ctx->stream));
+    if ((rc = finish_call(ctx))) return rc;
+    uint64_t covered;
+    std::memcpy(&covered, ctx->h_small + 1, 8);
+    if (covered < n_samples) {
+      a.nchunks = a.nchunks * 3 / 2 + 2;
+      continue;
+    }
+    if ((rc = begin_call(ctx))) return rc;
+    launch_temit(a, a.status, ctx->stream);
+    STOCHA_CUDA(cudaMemcpyAsync(dl, l.data(), dim * dim * 8, cudaMemcpyHostToDevice, ctx->stream));
+    launch_tcdf(a.raw, dl, n_samples, (int)dim, nu, u, ctx->stream);
+    STOCHA_CUDA(cudaGetLastError());
+    if ((rc = copy_to_host_populated(ctx->stream, out, u, n_samples * dim * 8))) return rc;
+    return finish_call(ctx);
+  }
+  return set_error(STOCHA_ERR_DEVICE, "sample stream parse did not cover the request");
 }
 
 }  // extern "C"

@@ -287,3 +287,30 @@ def test_gaussian_copula_validation(stocha):
         stocha.gaussian_copula(np.array([[1.0, 1.5], [1.5, 1.0]]), 10)
     with pytest.raises(TypeError):
         stocha.gaussian_copula([[1.0, 0.0], [0.0, 1.0]], 10)
+
+
+def test_student_t_copula_validation(stocha):
+    """student_t_copula's checks (lib.rs:570-572, copula/student_t.rs:141-149)."""
+    eye = np.eye(2)
+    for nu in (2.0, 1.0, -3.0):
+        with pytest.raises(ValueError, match="nu must be > 2"):
+            stocha.student_t_copula(eye, nu, 10)
+    with pytest.raises(ValueError, match="correlation matrix must be square"):
+        stocha.student_t_copula(np.ones((2, 3)), 5.0, 10)
+    with pytest.raises(ValueError, match="matrix is not positive-definite"):
+        stocha.student_t_copula(np.array([[1.0, 1.5], [1.5, 1.0]]), 5.0, 10)
+    with pytest.raises(TypeError):
+        stocha.student_t_copula([[1.0, 0.0], [0.0, 1.0]], 5.0, 10)
+
+
+def test_oracle_student_t_known_values(oracle):
+    """The oracle against the reference's unit tests (copula/student_t.rs:175-200):
+    CDF symmetry, and copula samples of shape (500, 2) inside (0, 1)."""
+    assert abs(oracle.student_t_cdf(0.0, 5.0) - 0.5) < 1e-6
+    assert abs(oracle.student_t_cdf(1.0, 5.0) + oracle.student_t_cdf(-1.0, 5.0) - 1.0) < 1e-5
+    # published t-distribution quantiles: P(T_5 <= 2.015048) = 0.95, P(T_10 <= 2.763769) = 0.99
+    assert abs(oracle.student_t_cdf(2.015048, 5.0) - 0.95) < 1e-5
+    assert abs(oracle.student_t_cdf(2.763769, 10.0) - 0.99) < 1e-5
+    u = oracle.student_t_copula(np.array([[1.0, 0.5], [0.5, 1.0]]), 5.0, 500, 42)
+    assert u.shape == (500, 2) and np.all((u > 0) & (u < 1))
+
