@@ -293,9 +293,11 @@ int stocha_var_cvar_device(stocha_ctx* ctx, const double* returns_dev, uint64_t 
 /* ------------------------------------------------------------- autotuner
  * No counterpart in the reference.  The fused FP32 pricing kernels have a
  * launch shape per model kind: the kernel form (variant 0: one path per
- * thread at a time; variant 1: ilp paths per thread in lockstep, 1 or 2),
- * threads per block (64/128/256) and grid waves (1 or 2 times the resident
- * blocks): 18 shapes.  stocha_autotune times every shape on the given model
+ * thread at a time; variant 1: ilp paths per thread in lockstep, 1 or 2;
+ * variant 2: one path per thread, the ziggurat fed one draw per warp-wide
+ * iteration so that wedge and tail attempts do not stall the warp), threads
+ * per block (64/128/256) and grid waves (1 or 2 times the resident blocks):
+ * 24 shapes.  stocha_autotune times every shape on the given model
  * and size (reps launches each, CUDA events on the context's stream) and
  * installs the fastest for that model kind; the table is process-wide.
  * Draws and per-path values do not depend on the shape; the grouping of the

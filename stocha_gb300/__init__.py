@@ -307,9 +307,10 @@ def _tune_dict(r) -> dict:
 
 def autotune(model: str, params: dict, steps: int = 252, n_paths: int = 1_000_000, reps: int = 3) -> dict:
     """Times every launch shape of the fused FP32 pricing kernel of ``model``
-    (kernel form: one path per thread at a time, or 1 or 2 paths per thread
-    in lockstep; threads per block 64/128/256; 1 or 2 waves of resident
-    blocks) on this size and installs the fastest for the model kind
+    (kernel form: one path per thread at a time, 1 or 2 paths per thread
+    in lockstep, or one path per thread with the sampler fed one draw per
+    warp-wide iteration; threads per block 64/128/256; 1 or 2 waves of
+    resident blocks) on this size and installs the fastest for the model kind
     (process-wide).  Returns the chosen shape with its time and the default
     shape's time (ms per launch)."""
     m = model_struct(model, params, steps, n_paths)

@@ -625,7 +625,7 @@ int stocha_tune_set(int32_t model, int32_t n_assets, int32_t block, int32_t ilp,
   if (slot < 0) return set_error(STOCHA_ERR_VALUE, "no fused FP32 kernel for this model");
   if (set_fused_tune(slot, FusedTune{block, ilp, waves, variant}))
     return set_error(STOCHA_ERR_VALUE,
-                     "block must be 64, 128 or 256; waves 1 or 2; variant 0 (ilp 1) or 1 (ilp 1 or 2)");
+                     "block must be 64, 128 or 256; waves 1 or 2; variant 0 or 2 (ilp 1) or 1 (ilp 1 or 2)");
   return STOCHA_OK;
 }
 
@@ -671,7 +671,7 @@ int stocha_autotune(stocha_ctx* ctx, const stocha_model* m, int32_t reps, stocha
   double best_ms = 1e300, default_ms = 0.0;
   int n = 0;
   rc = STOCHA_OK;
-  const int forms[3][2] = {{0, 1}, {1, 1}, {1, 2}};  // (variant, ilp)
+  const int forms[4][2] = {{0, 1}, {1, 1}, {1, 2}, {2, 1}};  // (variant, ilp)
   for (int b : {64, 128, 256})
     for (const auto& fm : forms)
       for (int waves : {1, 2}) {

@@ -7,13 +7,14 @@
 // Its consumption depends only on the draws, so the stream is cut into
 // chunks of C draws and each chunk is parsed from E candidate entry offsets
 // at once (k_tparse: samples starting in the chunk, and where the last one
-// ends).  One thread then chains the true entries chunk by chunk (k_tstitch;
-// a chunk whose entry lies beyond the candidates is parsed there, in order),
+// ends).  The true entries are then chained through groups of chunks
+// (k_tcompose, k_ttop, k_tfill; a chunk whose entry lies beyond the
+// candidates is parsed where it is met),
 // k_temit re-parses every chunk from its true entry and stores each sample's
 // chi-square and normals, and k_tcdf forms the uniforms
 // u = T_nu((L z)_j * sqrt(nu / chi2)) with the reference's Student-t CDF
 // (regularized incomplete beta by the modified-Lentz continued fraction,
-// Lanczos log-gamma; student_t.rs:6-91).  Every decision uses the
+// Lanczos log-gamma formed on the host; student_t.rs:6-91).  Every decision uses the
 // reference's FP64 values (exact normals; ln in the gamma test and the CDF
 // from the device libm).
 #include <cuda_runtime.h>
@@ -44,13 +45,18 @@ __device__ double sample_gamma(CountingGen& g, double d, double c, const Sampler
 }
 
 // One sample: chi-square (2 * gamma(nu / 2), student_t.rs:121-124) and dim
-// normals (z may be null: consumption only).
+// normals.  With z null only the consumption matters: the normals are then
+// drawn by the FP32 sampler, which consumes exactly the same draws without
+// FP64 work (the gamma's own normal keeps its exact FP64 value, which steers
+// the accept test).
 __device__ __forceinline__ double sample_one(CountingGen& g, const TParse& a, const SamplerCtx& sc,
                                              const ZigShared& zs, unsigned& err, double* z) {
   const double chi = 2.0 * sample_gamma(g, a.d, a.c, sc, zs, err);
   for (int j = 0; j < a.dim; ++j) {
-    const double v = normal_f64(g, sc, zs, err);
-    if (z) z[j] = v;
+    if (z)
+      z[j] = normal_f64(g, sc, zs, err);
+    else
+      (void)normal_f32(g, sc, zs, err);
   }
   return chi;
 }
@@ -90,36 +96,86 @@ __global__ void __launch_bounds__(128) k_tparse(const __grid_constant__ TParse a
   if (err) atomicOr(a.err, err);
 }
 
-// One thread: true entry of every chunk and the index of its first sample,
-// until n samples are covered.
-__global__ void k_tstitch(const __grid_constant__ TParse a) {
+// Carries (entry, count) through chunk c: the candidate table, a chunk that a
+// sample spans entirely, or a parse when the entry lies beyond the candidates.
+__device__ __forceinline__ void chunk_step(const TParse& a, uint64_t c, uint64_t& entry, uint64_t& count,
+                                           const SamplerCtx& sc, const ZigShared& zs, unsigned& err) {
+  if (entry >= a.C) {
+    entry -= a.C;
+    return;
+  }
+  if (entry < (uint64_t)a.E) {
+    count += a.counts[c * a.E + entry];
+    entry = a.exits[c * a.E + entry];
+    return;
+  }
+  const uint64_t lo = c * a.C;
+  uint32_t n;
+  entry = parse_span(a, lo + entry, lo + a.C, sc, zs, err, &n) - (lo + a.C);
+  count += n;
+}
+
+// The stitch runs in three passes over groups of G chunks, so that no thread
+// follows more than ~sqrt(chunks) dependent lookups:
+//   compose: per (group, candidate entry) the group's exit and sample count;
+//   top:     one thread chains the groups from entry 0 until n samples;
+//   fill:    per group, the true entry and first sample of each of its chunks.
+__global__ void __launch_bounds__(128) k_tcompose(const __grid_constant__ TParse a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx sc{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < a.ngroups * a.E) {
+    const uint64_t g = t / a.E;
+    uint64_t entry = t - g * a.E, count = 0;
+    const uint64_t c1 = min(a.nchunks, (g + 1) * a.G);
+    for (uint64_t c = g * a.G; c < c1; ++c) chunk_step(a, c, entry, count, sc, zs, err);
+    a.gexit[t] = entry;
+    a.gcount[t] = count;
+  }
+  if (err) atomicOr(a.err, err);
+}
+
+__global__ void k_ttop(const __grid_constant__ TParse a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
   if (threadIdx.x != 0) return;
   const SamplerCtx sc{a.tabs, a.tabs->r32, a.tabs->r};
   unsigned err = 0;
-  uint64_t entry = 0, base = 0, used = 0;
-  for (uint64_t c = 0; c < a.nchunks && base < a.n; ++c) {
-    a.entry[c] = entry;
-    a.first[c] = base;
-    uint64_t exit;
-    uint32_t cnt;
-    if (entry >= a.C) {  // a sample spans this whole chunk
-      cnt = 0;
-      exit = entry - a.C;
-    } else if (entry < (uint64_t)a.E) {
-      exit = a.exits[c * a.E + entry];
-      cnt = a.counts[c * a.E + entry];
-    } else {  // beyond the candidates: parse here
-      const uint64_t lo = c * a.C;
-      exit = parse_span(a, lo + entry, lo + a.C, sc, zs, err, &cnt) - (lo + a.C);
+  uint64_t entry = 0, base = 0, g = 0;
+  for (; g < a.ngroups && base < a.n; ++g) {
+    a.gentry[g] = entry;
+    a.gfirst[g] = base;
+    if (entry < (uint64_t)a.E) {
+      base += a.gcount[g * a.E + entry];
+      entry = a.gexit[g * a.E + entry];
+    } else {
+      const uint64_t c1 = min(a.nchunks, (g + 1) * a.G);
+      for (uint64_t c = g * a.G; c < c1; ++c) chunk_step(a, c, entry, base, sc, zs, err);
     }
-    base += cnt;
-    entry = exit;
-    used = c + 1;
   }
-  a.status[0] = used;
+  a.status[0] = min(a.nchunks, g * a.G);
   a.status[1] = base;
+  a.status[2] = g;
+  if (err) atomicOr(a.err, err);
+}
+
+__global__ void __launch_bounds__(128) k_tfill(const __grid_constant__ TParse a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx sc{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < a.status[2]) {
+    uint64_t entry = a.gentry[g], base = a.gfirst[g];
+    const uint64_t c1 = min(a.nchunks, (g + 1) * a.G);
+    for (uint64_t c = g * a.G; c < c1; ++c) {
+      a.entry[c] = entry;
+      a.first[c] = base;
+      chunk_step(a, c, entry, base, sc, zs, err);
+    }
+  }
   if (err) atomicOr(a.err, err);
 }
 
@@ -144,46 +200,41 @@ __global__ void __launch_bounds__(128) k_temit(const __grid_constant__ TParse a,
 }
 
 // ---- Student-t CDF (student_t.rs:6-91) ----
-__device__ double lgamma_lanczos(double x) {  // Lanczos, g = 7, nine coefficients
-  const double C[9] = {0.99999999999980993,  676.5203681218851,     -1259.1392167224028,
-                       771.32342877765313,   -176.61502916214059,   12.507343278686905,
-                       -0.13857109526572012, 9.9843695780195716e-6, 1.5056327351493116e-7};
-  const double PI = 3.14159265358979323846;
-  double refl = 0.0;
-  if (x < 0.5) {  // reflection, at most once for the arguments used here
-    refl = log(PI) - log(sin(PI * x));
-    x = 1.0 - x;
-    x -= 1.0;
-    double acc = C[0];
-    for (int i = 1; i < 9; ++i) acc += C[i] / (x + (double)i);
-    const double t = x + 7.0 + 0.5;
-    return refl - (0.5 * log(2.0 * PI) + (x + 0.5) * log(t) - t + log(acc));
-  }
-  x -= 1.0;
-  double acc = C[0];
-  for (int i = 1; i < 9; ++i) acc += C[i] / (x + (double)i);
-  const double t = x + 7.0 + 0.5;
-  return 0.5 * log(2.0 * PI) + (x + 0.5) * log(t) - t + log(acc);
+// 1/y for normal y > 0: the hardware's approximate FP64 reciprocal
+// (rcp.approx.ftz.f64) refined by two Newton-Raphson steps r += r (1 - y r),
+// each of which squares the relative error, to within an ulp or two of the
+// correctly rounded value.  Replaces the reference's divisions inside the
+// continued fraction: the values move by rounding only (~1e-16 relative per
+// step).
+__device__ __forceinline__ double recip_nr(double y) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(y));
+  double e = fma(-y, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-y, r, 1.0);
+  return fma(r, e, r);
 }
 
-__device__ double beta_cf(double x, double a, double b) {  // modified Lentz, student_t.rs:40-72
+// Modified Lentz continued fraction of the incomplete beta (student_t.rs:40-72).
+// The even and odd partial numerators are x times coefficients of m alone
+// (cf[2(m-1)], cf[2(m-1)+1]), formed once per call on the host.
+__device__ double beta_cf(double x, double a, double b, const double* __restrict__ cf) {
   const double EPS = 3e-7, FPMIN = 1e-30;
-  const double qab = a + b, qap = a + 1.0, qam = a - 1.0;
+  const double qab = a + b, qap = a + 1.0;
   double c = 1.0;
   double d = fmax(1.0 - qab * x / qap, FPMIN);
-  d = 1.0 / d;
+  d = recip_nr(d);
   double h = d;
   for (int m = 1; m <= 200; ++m) {
-    const double mf = (double)m, m2 = 2.0 * mf;
-    double aa = mf * (b - mf) * x / ((qam + m2) * (a + m2));
+    double aa = __ldg(cf + 2 * (m - 1)) * x;
     d = fmax(fabs(1.0 + aa * d), FPMIN);
-    c = fmax(fabs(1.0 + aa / c), FPMIN);
-    d = 1.0 / d;
+    c = fmax(fabs(1.0 + aa * recip_nr(c)), FPMIN);
+    d = recip_nr(d);
     h *= d * c;
-    aa = -(a + mf) * (qab + mf) * x / ((a + m2) * (qap + m2));
+    aa = __ldg(cf + 2 * (m - 1) + 1) * x;
     d = fmax(fabs(1.0 + aa * d), FPMIN);
-    c = fmax(fabs(1.0 + aa / c), FPMIN);
-    d = 1.0 / d;
+    c = fmax(fabs(1.0 + aa * recip_nr(c)), FPMIN);
+    d = recip_nr(d);
     const double del = d * c;
     h *= del;
     if (fabs(del - 1.0) < EPS) break;
@@ -191,7 +242,12 @@ __device__ double beta_cf(double x, double a, double b) {  // modified Lentz, st
   return h;
 }
 
-__device__ double ibeta(double x, double a, double b) {  // student_t.rs:19-31
+// student_t.rs:19-31.  log_beta = lgamma(a) + lgamma(b) - lgamma(a + b) is
+// the same for (a, b) and the flipped (b, a) (IEEE addition commutes), so the
+// host forms it once per call with the reference's Lanczos log-gamma.
+// cf holds the continued-fraction coefficients for (a, b) and, 400 doubles
+// on, for the flipped (b, a).
+__device__ double ibeta(double x, double a, double b, double log_beta, const double* __restrict__ cf) {
   if (x <= 0.0) return 0.0;
   if (x >= 1.0) return 1.0;
   bool flip = false;
@@ -201,15 +257,16 @@ __device__ double ibeta(double x, double a, double b) {  // student_t.rs:19-31
     const double t = a;
     a = b;
     b = t;
+    cf += 400;
   }
-  const double log_beta = lgamma_lanczos(a) + lgamma_lanczos(b) - lgamma_lanczos(a + b);
   const double front = exp(a * log(x) + b * log(1.0 - x) - log_beta) / a;
-  const double v = front * beta_cf(x, a, b);
+  const double v = front * beta_cf(x, a, b, cf);
   return flip ? 1.0 - v : v;
 }
 
 __global__ void __launch_bounds__(256) k_tcdf(const double* __restrict__ raw, const double* __restrict__ L,
-                                              uint64_t n, int dim, double nu, double* __restrict__ u) {
+                                              uint64_t n, int dim, double nu, double log_beta,
+                                              const double* __restrict__ cf, double* __restrict__ u) {
   const uint64_t total = n * (uint64_t)dim;
   for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t i = e / (uint64_t)dim;
@@ -220,7 +277,7 @@ __global__ void __launch_bounds__(256) k_tcdf(const double* __restrict__ raw, co
     for (int k = 0; k <= j; ++k) x += L[j * dim + k] * row[1 + k];
     const double xs = x * scale;
     const double z = nu / (nu + xs * xs);
-    const double ib = ibeta(z, nu / 2.0, 0.5);
+    const double ib = ibeta(z, nu / 2.0, 0.5, log_beta, cf);
     u[e] = xs >= 0.0 ? 1.0 - 0.5 * ib : 0.5 * ib;
   }
 }
@@ -234,18 +291,24 @@ void launch_tparse(const TParse& a, cudaStream_t st) {
   k_tparse<<<(unsigned)(g ? g : 1), 128, 0, st>>>(a);
 }
 
-void launch_tstitch(const TParse& a, cudaStream_t st) { k_tstitch<<<1, 32, 0, st>>>(a); }
+void launch_tstitch(const TParse& a, cudaStream_t st) {
+  const uint64_t threads = a.ngroups * (uint64_t)a.E;
+  k_tcompose<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(a);
+  k_ttop<<<1, 32, 0, st>>>(a);
+  k_tfill<<<(unsigned)((a.ngroups + 127) / 128), 128, 0, st>>>(a);
+}
 
 void launch_temit(const TParse& a, const uint64_t* status, cudaStream_t st) {
   uint64_t g = (a.nchunks + 127) / 128;
   k_temit<<<(unsigned)(g ? g : 1), 128, 0, st>>>(a, status);
 }
 
-void launch_tcdf(const double* raw, const double* L, uint64_t n, int dim, double nu, double* u, cudaStream_t st) {
+void launch_tcdf(const double* raw, const double* L, uint64_t n, int dim, double nu, double log_beta,
+                 const double* cf, double* u, cudaStream_t st) {
   const uint64_t total = n * (uint64_t)dim;
   uint64_t g = (total + 255) / 256;
   if (g > 152ull * 32) g = 152ull * 32;
-  k_tcdf<<<(unsigned)(g ? g : 1), 256, 0, st>>>(raw, L, n, dim, nu, u);
+  k_tcdf<<<(unsigned)(g ? g : 1), 256, 0, st>>>(raw, L, n, dim, nu, log_beta, cf, u);
 }
 
 }  // namespace stocha

@@ -21,13 +21,23 @@ struct TParse {
   uint32_t* counts;     // nchunks * E: samples starting in the chunk
   uint64_t* entry;      // nchunks: true entry offset
   uint64_t* first;      // nchunks: index of the chunk's first sample
-  uint64_t* status;     // [0] chunks used, [1] samples covered
+  uint64_t* status;     // [0] chunks used, [1] samples covered, [2] groups used
   double* raw;          // n * (dim + 1): chi-square, then the dim normals
+  // groups of G consecutive chunks, composed per candidate entry
+  uint64_t G, ngroups;
+  uint64_t* gexit;      // ngroups * E: exit of the group's last chunk
+  uint64_t* gcount;     // ngroups * E: samples starting in the group
+  uint64_t* gentry;     // ngroups: true entry offset of the group's first chunk
+  uint64_t* gfirst;     // ngroups: index of the group's first sample
 };
 
 void launch_tparse(const TParse& a, cudaStream_t st);
 void launch_tstitch(const TParse& a, cudaStream_t st);
 void launch_temit(const TParse& a, const uint64_t* status, cudaStream_t st);
-void launch_tcdf(const double* raw, const double* L, uint64_t n, int dim, double nu, double* u, cudaStream_t st);
+// cf: 800 doubles, the continued-fraction coefficients of the incomplete
+// beta for (nu/2, 1/2) then (1/2, nu/2): per m = 1..200 the even and odd
+// partial numerators divided by x.
+void launch_tcdf(const double* raw, const double* L, uint64_t n, int dim, double nu, double log_beta,
+                 const double* cf, double* u, cudaStream_t st);
 
 }  // namespace stocha

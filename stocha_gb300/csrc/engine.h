@@ -86,7 +86,7 @@ struct FusedTune {
   int block;    // threads per block: 64, 128 or 256
   int ilp;      // paths per thread in lockstep: 1 or 2 (lockstep form)
   int waves;    // grid = waves * resident blocks (1 or 2)
-  int variant;  // 0: per-path loop kernel (ilp 1); 1: lockstep kernel
+  int variant;  // 0: per-path loop kernel (ilp 1); 1: lockstep kernel; 2: warp-uniform sampler feed (ilp 1)
 };
 constexpr int kTuneSlots = 7;
 int tune_slot(int model, int na);  // -1: no fused FP32 kernel for this model

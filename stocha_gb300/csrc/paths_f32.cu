@@ -415,6 +415,208 @@ __global__ void __launch_bounds__(256) k_multi_fused(const __grid_constant__ Pat
   if (err) atomicOr(a.err, err);
 }
 
+// ------------------------------------------------ fused, warp-uniform -------
+// The same fused pricing with the ziggurat fed one draw per iteration
+// (zig_feed): each iteration every lane of the warp takes one generator step
+// and feeds it to its own sampler state; a lane that completes a normal hands
+// it to the model.  A warp prices 32 consecutive rows together and iterates
+// until all 32 have their normals (a lane that is done keeps stepping a
+// stream nobody reads).  Draws and values per path are those of the kernels
+// above; only the interleaving of lanes changes.
+
+// Rows of one warp: base (warp-uniform) + lane.  A lane past the end runs on
+// the first row's stream and contributes nothing.
+struct WarpRow {
+  bool ok, neg;
+  PcgGen s;
+};
+
+__device__ __forceinline__ WarpRow warp_row(const PathLaunch& a, uint64_t base) {
+  WarpRow r;
+  const uint64_t lrow = base + (threadIdx.x & 31u);
+  r.ok = lrow < a.rows;
+  const uint64_t row = a.row_begin + (r.ok ? lrow : base);
+  r.neg = row >= a.base_paths;
+  r.s = PcgGen{pcg_path_state(a.ss, r.neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
+  return r;
+}
+
+// Iteration bound of one warp's rows: far above the ~1.03 draws per normal
+// (a warp that reaches it flags kErrZigAttempts and stops).  Counts are
+// 32-bit: the launcher sends only steps * assets < 2^24 here.
+__device__ __forceinline__ uint32_t uf_cap(uint32_t normals) { return 64 * normals + 4096; }
+
+// Calls feed() (one draw per lane) in groups of kUfUnroll until every lane's
+// count has reached its need; the warp vote runs once per group.
+constexpr int kUfUnroll = 4;
+template <class F>
+__device__ __forceinline__ void uf_drive(const uint32_t& cnt, uint32_t need, uint32_t cap, unsigned& err, F&& feed) {
+  uint32_t it = 0;
+#pragma unroll 1
+  while (__any_sync(0xFFFFFFFFu, cnt < need)) {
+    if (it >= cap) {
+      err |= kErrZigAttempts;
+      break;
+    }
+#pragma unroll
+    for (int j = 0; j < kUfUnroll; ++j) feed();
+    it += kUfUnroll;
+  }
+}
+
+// GBM (NA = 0) and multi-GBM with NA assets: only the per-asset sums of the
+// normals matter.  The sum being filled is always w[0]; after each normal the
+// sums rotate, so after steps * NA normals they are back in asset order.
+template <int NA>
+__global__ void __launch_bounds__(256) k_gbm_uf(const __grid_constant__ PathLaunch a) {
+  constexpr int N = NA > 0 ? NA : 1;
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  unsigned err = 0;
+  Kahan acc[N], acc2[N];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  const uint32_t need_all = (uint32_t)a.steps * N, cap = uf_cap(need_all);
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
+    WarpRow r = warp_row(a, base);
+    Kahan w[N];
+    ZigLane q;
+    const uint32_t need = r.ok ? need_all : 0;
+    uint32_t cnt = 0;
+    uf_drive(cnt, need, cap, err, [&]() {
+      float z;
+      if (zig_feed(q, r.s.next(), c, zs, z) && cnt < need) {
+        w[0].add(r.neg ? -z : z);
+        ++cnt;
+        if constexpr (N > 1) {
+          const Kahan t = w[0];
+#pragma unroll
+          for (int i = 0; i + 1 < N; ++i) w[i] = w[i + 1];
+          w[N - 1] = t;
+        }
+      }
+    });
+    if (r.ok) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        float lg;
+        float s0;
+        if constexpr (NA == 0) {
+          lg = fmaf(f.g_diff, w[0].value(), f.g_kdrift);
+          s0 = f.g_s0;
+        } else {
+          float eps = 0.0f;
+#pragma unroll
+          for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
+          lg = fmaf(f.a_diff[i], eps, f.a_kdrift[i]);
+          s0 = f.a_s0[i];
+        }
+        const float p = payoff_f32(s0 * expf(lg), f.strike, a.payoff);
+        acc[i].add(p);
+        acc2[i].add(p * p);
+      }
+    }
+  }
+  store_partials<N>(a, acc, acc2);
+  if (err) atomicOr(a.err, err);
+}
+
+// Heston (Euler): normals pair up as (dw1, dz) of one step.
+__global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  const float rho = f.h_rho, rho_comp = f.h_rho_comp, kappa_dt = f.h_kdt, theta = f.h_theta;
+  const float xi_sdt = f.h_xsdt, sdt = f.h_sdt, mu_dt = f.h_mudt, nhdt = f.h_nhdt;
+  unsigned err = 0;
+  Kahan acc[1], acc2[1];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  const uint32_t cap = uf_cap(2 * (uint32_t)a.steps);
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
+    WarpRow r = warp_row(a, base);
+    ZigLane q;
+    Kahan lg;
+    float v = f.h_v0, dw1 = 0.0f;
+    bool half = false;
+    const uint32_t need = r.ok ? (uint32_t)a.steps : 0;
+    uint32_t cnt = 0;
+    uf_drive(cnt, need, cap, err, [&]() {
+      float z;
+      if (zig_feed(q, r.s.next(), c, zs, z) && cnt < need) {
+        if (!half) {
+          dw1 = z;
+          half = true;
+        } else {
+          const float dw2 = fmaf(rho, dw1, rho_comp * z);
+          const float v_plus = fmaxf(v, 0.0f);
+          const float sqrt_v = sqrtf(v_plus);
+          v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
+          lg.add(fmaf(nhdt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
+          half = false;
+          ++cnt;
+        }
+      }
+    });
+    if (r.ok) {
+      const float p = payoff_f32(f.h_s0 * expf(lg.value()), f.strike, a.payoff);
+      acc[0].add(p);
+      acc2[0].add(p * p);
+    }
+  }
+  store_partials<1>(a, acc, acc2);
+  if (err) atomicOr(a.err, err);
+}
+
+// Merton: after the diffusion normal of a step the lane takes the jump
+// uniform at once (a second generator step in the same iteration); on a jump
+// its next normal is the jump size.
+__global__ void __launch_bounds__(256) k_merton_uf(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  const float mu_j = f.m_mu_j, sigma_j = f.m_sigma_j;
+  const uint64_t thr = a.merton.jump_thr;
+  unsigned err = 0;
+  Kahan acc[1], acc2[1];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  const uint32_t cap = uf_cap(2 * (uint32_t)a.steps);
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
+    WarpRow r = warp_row(a, base);
+    ZigLane q;
+    Kahan w;
+    float jumps = 0.0f;
+    bool in_jump = false;
+    const uint32_t need = r.ok ? (uint32_t)a.steps : 0;
+    uint32_t cnt = 0;
+    uf_drive(cnt, need, cap, err, [&]() {
+      float z;
+      if (zig_feed(q, r.s.next(), c, zs, z) && cnt < need) {
+        if (in_jump) {
+          jumps += fmaf(sigma_j, z, mu_j);
+          in_jump = false;
+          ++cnt;
+        } else {
+          w.add(z);
+          if ((r.s.next() >> 11) < thr)
+            in_jump = true;
+          else
+            ++cnt;
+        }
+      }
+    });
+    if (r.ok) {
+      const float p = payoff_f32(f.m_s0 * expf(fmaf(f.m_diff, w.value(), f.m_kdrift) + jumps), f.strike, a.payoff);
+      acc[0].add(p);
+      acc2[0].add(p * p);
+    }
+  }
+  store_partials<1>(a, acc, acc2);
+  if (err) atomicOr(a.err, err);
+}
+
 // Tuning table: per model kind (gbm, heston, merton, multi-GBM with 1..4
 // assets) the block size, ILP and grid waves of the fused launch.
 FusedTune g_tune[kTuneSlots] = {{256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0},
@@ -430,6 +632,17 @@ const void* fused_kernel(int slot, int ilp, int variant) {
       case 4: return (const void*)k_multi_gbm_f32<2, false>;
       case 5: return (const void*)k_multi_gbm_f32<3, false>;
       default: return (const void*)k_multi_gbm_f32<4, false>;
+    }
+  }
+  if (variant == 2) {  // warp-uniform sampler feed (one path per thread)
+    switch (slot) {
+      case 0: return (const void*)k_gbm_uf<0>;
+      case 1: return (const void*)k_heston_uf;
+      case 2: return (const void*)k_merton_uf;
+      case 3: return (const void*)k_gbm_uf<1>;
+      case 4: return (const void*)k_gbm_uf<2>;
+      case 5: return (const void*)k_gbm_uf<3>;
+      default: return (const void*)k_gbm_uf<4>;
     }
   }
   const bool two = ilp == 2;
@@ -469,7 +682,7 @@ FusedTune get_fused_tune(int slot) {
 int set_fused_tune(int slot, FusedTune t) {
   if (slot < 0 || slot >= kTuneSlots) return -1;
   if ((t.block != 64 && t.block != 128 && t.block != 256) || (t.ilp != 1 && t.ilp != 2) || t.waves < 1 ||
-      t.waves > 2 || (t.variant != 0 && t.variant != 1) || (t.variant == 0 && t.ilp != 1))
+      t.waves > 2 || t.variant < 0 || t.variant > 2 || (t.variant != 1 && t.ilp != 1))
     return -1;
   g_tune[slot] = t;
   return 0;
@@ -484,7 +697,9 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
   if (!store && slot >= 0 && !(L.model == kHeston && L.heston.scheme != 0)) {
     // fused pricing: tuned block size, ILP and waves of resident blocks
     const FusedTune t = g_tune[slot];
-    const void* fn = fused_kernel(slot, t.ilp, t.variant);
+    // the warp-uniform form counts normals in 32 bits
+    const int variant = t.variant == 2 && L.steps >= (1ull << 22) ? 0 : t.variant;
+    const void* fn = fused_kernel(slot, t.ilp, variant);
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, t.block, 0) != cudaSuccess || per_sm < 1)
       per_sm = 1;

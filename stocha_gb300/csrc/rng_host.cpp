@@ -367,6 +367,21 @@ int stocha_gaussian_copula(stocha_ctx* ctx, const double* corr, size_t rows, siz
   return finish_call(ctx);  // l outlives the copy (synchronous)
 }
 
+// Log-gamma by the Lanczos approximation, g = 7, nine coefficients
+// (copula/student_t.rs:74-91), for the incomplete beta's log B(a, b).
+static double lgamma_lanczos(double x) {
+  static const double C[9] = {0.99999999999980993,  676.5203681218851,     -1259.1392167224028,
+                              771.32342877765313,   -176.61502916214059,   12.507343278686905,
+                              -0.13857109526572012, 9.9843695780195716e-6, 1.5056327351493116e-7};
+  const double pi = 3.14159265358979323846;
+  if (x < 0.5) return std::log(pi) - std::log(std::sin(pi * x)) - lgamma_lanczos(1.0 - x);
+  x -= 1.0;
+  double acc = C[0];
+  for (int i = 1; i < 9; ++i) acc += C[i] / (x + (double)i);
+  const double t = x + 7.0 + 0.5;
+  return 0.5 * std::log(2.0 * pi) + (x + 0.5) * std::log(t) - t + std::log(acc);
+}
+
 int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, size_t cols, double nu,
                             uint64_t n_samples, uint64_t seed, double* out) {
   if (nu <= 2.0) return set_error(STOCHA_ERR_VALUE, "nu must be > 2");  // lib.rs:570-572 (NaN passes, as there)
@@ -409,6 +424,7 @@ int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, si
   a.dim = (int)dim;
   a.E = (int)std::min<size_t>(2 * dim + 16, a.C);
   const double shape = nu / 2.0;  // student_t.rs:121-124, 102-103
+  std::vector<double> cf_host(800);
   a.d = shape - 1.0 / 3.0;
   a.c = 1.0 / std::sqrt(9.0 * a.d);
   // ~2.1 draws for the chi-square and 1.03 per normal
@@ -421,9 +437,17 @@ int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, si
     const size_t o_entry = (o_counts + nc * a.E * 4 + 7) & ~(size_t)7;
     const size_t o_first = o_entry + nc * 8;
     const size_t o_status = o_first + nc * 8;
-    const size_t o_raw = (o_status + 64 + 255) & ~(size_t)255;
+    a.G = 8;
+    while (a.G * a.G < nc) a.G *= 2;
+    a.ngroups = (nc + a.G - 1) / a.G;
+    const size_t o_gexit = o_status + 64;
+    const size_t o_gcount = o_gexit + a.ngroups * a.E * 8;
+    const size_t o_gentry = o_gcount + a.ngroups * a.E * 8;
+    const size_t o_gfirst = o_gentry + a.ngroups * 8;
+    const size_t o_raw = (o_gfirst + a.ngroups * 8 + 255) & ~(size_t)255;
     const size_t o_l = (o_raw + n_samples * (dim + 1) * 8 + 255) & ~(size_t)255;
-    const size_t o_u = (o_l + dim * dim * 8 + 255) & ~(size_t)255;
+    const size_t o_cf = (o_l + dim * dim * 8 + 255) & ~(size_t)255;
+    const size_t o_u = (o_cf + 800 * 8 + 255) & ~(size_t)255;
     const size_t bytes = o_u + n_samples * dim * 8;
     if ((rc = ensure_buf(ctx, ctx->aux, bytes))) return rc;
     char* base = (char*)ctx->aux.ptr;
@@ -432,6 +456,10 @@ int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, si
     a.entry = (uint64_t*)(base + o_entry);
     a.first = (uint64_t*)(base + o_first);
     a.status = (uint64_t*)(base + o_status);
+    a.gexit = (uint64_t*)(base + o_gexit);
+    a.gcount = (uint64_t*)(base + o_gcount);
+    a.gentry = (uint64_t*)(base + o_gentry);
+    a.gfirst = (uint64_t*)(base + o_gfirst);
     a.raw = (double*)(base + o_raw);
     double* dl = (double*)(base + o_l);
     double* u = (double*)(base + o_u);
@@ -450,7 +478,20 @@ int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, si
     if ((rc = begin_call(ctx))) return rc;
     launch_temit(a, a.status, ctx->stream);
     STOCHA_CUDA(cudaMemcpyAsync(dl, l.data(), dim * dim * 8, cudaMemcpyHostToDevice, ctx->stream));
-    launch_tcdf(a.raw, dl, n_samples, (int)dim, nu, u, ctx->stream);
+    const double a2 = nu / 2.0;
+    const double log_beta = lgamma_lanczos(a2) + lgamma_lanczos(0.5) - lgamma_lanczos(a2 + 0.5);
+    // continued-fraction coefficients (student_t.rs:48,54) for (a2, 1/2) and (1/2, a2)
+    for (int flip = 0; flip < 2; ++flip) {
+      const double A = flip ? 0.5 : a2, B = flip ? a2 : 0.5;
+      for (int m = 1; m <= 200; ++m) {
+        const double mf = m, m2 = 2.0 * mf;
+        cf_host[flip * 400 + 2 * (m - 1)] = mf * (B - mf) / ((A - 1.0 + m2) * (A + m2));
+        cf_host[flip * 400 + 2 * (m - 1) + 1] = -(A + mf) * (A + B + mf) / ((A + m2) * (A + 1.0 + m2));
+      }
+    }
+    double* dcf = (double*)(base + o_cf);
+    STOCHA_CUDA(cudaMemcpyAsync(dcf, cf_host.data(), 800 * 8, cudaMemcpyHostToDevice, ctx->stream));
+    launch_tcdf(a.raw, dl, n_samples, (int)dim, nu, log_beta, dcf, u, ctx->stream);
     STOCHA_CUDA(cudaGetLastError());
     if ((rc = copy_to_host_populated(ctx->stream, out, u, n_samples * dim * 8))) return rc;
     return finish_call(ctx);

@@ -230,7 +230,10 @@ def test_tune_table_host_logic(stocha):
         stocha.tune_set("gbm", 128, 2, 2, variant=1)
         got = stocha.tune_get("gbm")
         assert (got["block"], got["ilp"], got["waves"], got["variant"]) == (128, 2, 2, 1)
-        for bad in [(512, 1, 1, 1), (256, 3, 1, 1), (256, 1, 0, 1), (256, 1, 3, 1), (256, 2, 1, 0), (256, 1, 1, 2)]:
+        stocha.tune_set("gbm", 64, 1, 1, variant=2)
+        assert stocha.tune_get("gbm")["variant"] == 2
+        for bad in [(512, 1, 1, 1), (256, 3, 1, 1), (256, 1, 0, 1), (256, 1, 3, 1), (256, 2, 1, 0), (256, 2, 1, 2),
+                    (256, 1, 1, 3), (256, 1, 1, -1)]:
             with pytest.raises(ValueError):
                 stocha.tune_set("gbm", bad[0], bad[1], bad[2], variant=bad[3])
         with pytest.raises(ValueError):
