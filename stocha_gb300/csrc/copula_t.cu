@@ -200,21 +200,6 @@ __global__ void __launch_bounds__(128) k_temit(const __grid_constant__ TParse a,
 }
 
 // ---- Student-t CDF (student_t.rs:6-91) ----
-// 1/y for normal y > 0: the hardware's approximate FP64 reciprocal
-// (rcp.approx.ftz.f64) refined by two Newton-Raphson steps r += r (1 - y r),
-// each of which squares the relative error, to within an ulp or two of the
-// correctly rounded value.  Replaces the reference's divisions inside the
-// continued fraction: the values move by rounding only (~1e-16 relative per
-// step).
-__device__ __forceinline__ double recip_nr(double y) {
-  double r;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(y));
-  double e = fma(-y, r, 1.0);
-  r = fma(r, e, r);
-  e = fma(-y, r, 1.0);
-  return fma(r, e, r);
-}
-
 // Modified Lentz continued fraction of the incomplete beta (student_t.rs:40-72).
 // The even and odd partial numerators are x times coefficients of m alone
 // (cf[2(m-1)], cf[2(m-1)+1]), formed once per call on the host.

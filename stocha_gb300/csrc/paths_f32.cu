@@ -62,12 +62,17 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       float z = normal_f32(s, c, zs, err);
-      w.add(neg ? -z : z);
-      kf += 1.0f;
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value())));
+      if (kStore) {
+        w.add(neg ? -z : z);
+        kf += 1.0f;
+        store32(a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value())));
+      } else {
+        w.add(z);  // the antithetic sign is applied to the sum (negation is exact)
+      }
     }
     if (!kStore) {
-      float sT = s0 * expf(fmaf(diffusion, w.value(), a.f32.g_kdrift));
+      const float sum = neg ? -w.value() : w.value();
+      float sT = s0 * expf(fmaf(diffusion, sum, a.f32.g_kdrift));
       float p = payoff_f32(sT, strike, a.payoff);
       acc.add(p);
       acc2.add(p * p);
@@ -101,7 +106,7 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
 #pragma unroll
       for (int i = 0; i < na; ++i) {
         float z = normal_f32(s, c, zs, err);
-        w[i].add(neg ? -z : z);
+        w[i].add(kStore && neg ? -z : z);  // fused: the sign is applied to the sums
       }
       kf += 1.0f;
       if (kStore) {
@@ -120,7 +125,7 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
       for (int i = 0; i < na; ++i) {
         float eps = 0.0f;
 #pragma unroll
-        for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
+        for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], neg ? -w[m].value() : w[m].value(), eps);
         float lg = fmaf(f.a_diff[i], eps, f.a_kdrift[i]);
         float p = payoff_f32(f.a_s0[i] * expf(lg), f.strike, a.payoff);
         acc[i].add(p);
@@ -487,7 +492,7 @@ __global__ void __launch_bounds__(256) k_gbm_uf(const __grid_constant__ PathLaun
     uf_drive(cnt, need, cap, err, [&]() {
       float z;
       if (zig_feed(q, r.s.next(), c, zs, z) && cnt < need) {
-        w[0].add(r.neg ? -z : z);
+        w[0].add(z);  // the antithetic sign is applied to the sums
         ++cnt;
         if constexpr (N > 1) {
           const Kahan t = w[0];
@@ -503,12 +508,13 @@ __global__ void __launch_bounds__(256) k_gbm_uf(const __grid_constant__ PathLaun
         float lg;
         float s0;
         if constexpr (NA == 0) {
-          lg = fmaf(f.g_diff, w[0].value(), f.g_kdrift);
+          lg = fmaf(f.g_diff, r.neg ? -w[0].value() : w[0].value(), f.g_kdrift);
           s0 = f.g_s0;
         } else {
           float eps = 0.0f;
 #pragma unroll
-          for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
+          for (int m = 0; m <= i; ++m)
+            eps = fmaf(f.a_L[i * kMaxAssets + m], r.neg ? -w[m].value() : w[m].value(), eps);
           lg = fmaf(f.a_diff[i], eps, f.a_kdrift[i]);
           s0 = f.a_s0[i];
         }

@@ -72,8 +72,17 @@ __global__ void __launch_bounds__(256) k_tail_sum(const double* __restrict__ r, 
                                                   const SelectState* __restrict__ st, double* __restrict__ part) {
   const uint64_t key = st->prefix;
   double s = 0.0;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-    if (loss_key(r[i]) > key) s += -r[i];
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const double v = r[i];
+    // Only the tail (a fraction 1 - confidence of the returns) is added.  A
+    // warp issues the FP64 add (1/64 of the FP32 rate on GB300) only when one
+    // of its lanes holds a tail loss; a predicated add would occupy the FP64
+    // pipe for every element.
+    const bool take = loss_key(v) > key;
+    // (volatile: the subtraction must stay inside the branch, not be
+    // speculated and selected)
+    if (__any_sync(__activemask(), take) && take) asm volatile("sub.rn.f64 %0, %0, %1;" : "+d"(s) : "d"(v));
+  }
   block_sum2_store(s, 0.0, part + 2 * (uint64_t)blockIdx.x);
 }
 

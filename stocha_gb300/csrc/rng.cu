@@ -219,10 +219,15 @@ void launch_rng_emit(const StreamSpec& ss, const ZigTables* tabs, uint64_t nchun
 // One thread per output element (i, j): the reference's running sum
 // x_j = sum_{k<=j} L[j,k] z_k in k order (gaussian.rs:60-66; this unit is
 // compiled without FMA contraction), then its normal CDF
-// (dist/normal_cdf.rs:3-22, Abramowitz-Stegun 26.2.17).
+// (dist/normal_cdf.rs:3-22, Abramowitz-Stegun 26.2.17).  The CDF's FP64
+// division and exp (GB300 runs FP64 at 1/64 of the FP32 rate) are the
+// Newton reciprocal and the table-driven exponential: pdf = exp(-x^2/2) /
+// sqrt(2 pi) becomes (1 / sqrt(2 pi)) * exp(-x^2/2), within ~3 ulp of it.
 __global__ void __launch_bounds__(256) k_copula_gaussian(const double* __restrict__ z, const double* __restrict__ L,
-                                                         uint64_t n, int dim, double sqrt_2pi,
-                                                         double* __restrict__ u) {
+                                                         uint64_t n, int dim, const ZigTables* __restrict__ tabs,
+                                                         double inv_sqrt_2pi, double* __restrict__ u) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, tabs, true);
   const uint64_t total = n * (uint64_t)dim;
   for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
     const uint64_t i = e / (uint64_t)dim;
@@ -230,22 +235,22 @@ __global__ void __launch_bounds__(256) k_copula_gaussian(const double* __restric
     const double* zi = z + i * (uint64_t)dim;
     double x = 0.0;
     for (int k = 0; k <= j; ++k) x += L[j * dim + k] * zi[k];
-    const double t = 1.0 / (1.0 + 0.2316419 * fabs(x));
+    const double t = recip_nr(1.0 + 0.2316419 * fabs(x));
     const double poly =
         t * (0.319381530 + t * (-0.356563782 + t * (1.781477937 + t * (-1.821255978 + t * 1.330274429))));
-    const double pdf = exp(-0.5 * x * x) / sqrt_2pi;
+    const double pdf = mul_exp(inv_sqrt_2pi, -0.5 * x * x, zs);
     const double cdf_pos = 1.0 - pdf * poly;
     u[e] = x >= 0.0 ? cdf_pos : 1.0 - cdf_pos;
   }
 }
 
-void launch_copula_gaussian(const double* z, const double* L, uint64_t n, int dim, double sqrt_2pi, double* u,
-                            cudaStream_t st) {
+void launch_copula_gaussian(const double* z, const double* L, uint64_t n, int dim, const ZigTables* tabs,
+                            double inv_sqrt_2pi, double* u, cudaStream_t st) {
   const uint64_t total = n * (uint64_t)dim;
   uint64_t g = (total + 255) / 256;
   if (g > 152ull * 32) g = 152ull * 32;
   if (g < 1) g = 1;
-  k_copula_gaussian<<<(unsigned)g, 256, 0, st>>>(z, L, n, dim, sqrt_2pi, u);
+  k_copula_gaussian<<<(unsigned)g, 256, 0, st>>>(z, L, n, dim, tabs, inv_sqrt_2pi, u);
 }
 
 }  // namespace stocha

@@ -360,8 +360,8 @@ int stocha_gaussian_copula(stocha_ctx* ctx, const double* corr, size_t rows, siz
   double* dl = (double*)((char*)ctx->aux.ptr + ((nz * 8 + 255) & ~(size_t)255));
   if ((rc = begin_call(ctx))) return rc;
   STOCHA_CUDA(cudaMemcpyAsync(dl, l.data(), dim * dim * 8, cudaMemcpyHostToDevice, ctx->stream));
-  launch_copula_gaussian((const double*)ctx->out.ptr, dl, n_samples, (int)dim, std::sqrt(2.0 * M_PI), u,
-                         ctx->stream);
+  launch_copula_gaussian((const double*)ctx->out.ptr, dl, n_samples, (int)dim, ctx->d_tabs,
+                         1.0 / std::sqrt(2.0 * M_PI), u, ctx->stream);
   STOCHA_CUDA(cudaGetLastError());
   if ((rc = copy_to_host_populated(ctx->stream, out, u, nz * 8))) return rc;
   return finish_call(ctx);  // l outlives the copy (synchronous)
@@ -420,9 +420,15 @@ int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, si
   a.tabs = ctx->d_tabs;
   a.err = ctx->d_err;
   a.n = n_samples;
-  a.C = 1024;
+  // 256 draws (~40 samples at dim 4) per chunk: the emit pass runs one thread
+  // per chunk, so shorter chunks give it enough threads to hide latency
+  a.C = 256;
   a.dim = (int)dim;
-  a.E = (int)std::min<size_t>(2 * dim + 16, a.C);
+  // A sample takes dim + 2 draws plus a few on rejections, so the true entry
+  // of a chunk (the overshoot of the sample that straddles its start) lies
+  // below dim + 8 except after 7 or more extra draws in that one sample; such
+  // an entry is parsed where the stitch meets it.
+  a.E = (int)std::min<size_t>(dim + 8, a.C);
   const double shape = nu / 2.0;  // student_t.rs:121-124, 102-103
   std::vector<double> cf_host(800);
   a.d = shape - 1.0 / 3.0;

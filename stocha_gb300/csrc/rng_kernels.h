@@ -20,9 +20,9 @@ void launch_rng_emit(const StreamSpec& ss, const ZigTables* tabs, uint64_t nchun
                      double loc, double scale, double* out, uint64_t* final_pos, unsigned* err, cudaStream_t st);
 
 // Gaussian copula rows: u[i, j] = Phi(sum_{k<=j} L[j, k] z[i, k]) with the
-// reference's normal CDF (dist/normal_cdf.rs, A&S 26.2.17); sqrt_2pi is the
-// host's sqrt(2 pi).
-void launch_copula_gaussian(const double* z, const double* L, uint64_t n, int dim, double sqrt_2pi, double* u,
-                            cudaStream_t st);
+// reference's normal CDF (dist/normal_cdf.rs, A&S 26.2.17); inv_sqrt_2pi is
+// 1 / the host's sqrt(2 pi); tabs supplies the exponential's table.
+void launch_copula_gaussian(const double* z, const double* L, uint64_t n, int dim, const ZigTables* tabs,
+                            double inv_sqrt_2pi, double* u, cudaStream_t st);
 
 }  // namespace stocha

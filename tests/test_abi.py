@@ -54,6 +54,8 @@ def test_fast_path_thresholds_match_fp64_compare(stocha):
                 fast = (float(m) * two53) * X[L] < X[L + 1]  # normal.rs:25-27
                 assert fast == (m < t), (L, m, t)
     assert int(thr[255]) == 0  # X[256] = 0: layer 255 never takes the fast path
+    # the kernels compare the raw draw with thr * 2^11, exact only while thr < 2^53
+    assert int(thr.max()) < 2**53
 
 
 def test_validation_messages(stocha):
