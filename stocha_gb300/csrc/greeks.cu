@@ -167,7 +167,7 @@ __device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, con
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
       const float vp = fmaxf(v[t], 0.0f);
-      const float sv = sqrtf(vp);
+      const float sv = sqrt_approx(vp);
       v[t] += fmaf(I.hkdt[t], I.htheta - vp, I.hxsdt[t] * sv * dw2);
       lg[t].add(fmaf(I.hnhdt[t], vp, I.hmudt[t]) + sv * I.hsdt[t] * dw1);
     }

@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(256) k_heston_euler_f32(const __grid_constant_
       float dz = normal_f32(s, c, zs, err);
       float dw2 = fmaf(rho, dw1, rho_comp * dz);
       float v_plus = fmaxf(v, 0.0f);
-      float sqrt_v = sqrtf(v_plus);
+      float sqrt_v = sqrt_approx(v_plus);
       v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
       lg.add(fmaf(-half_dt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
       if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(lg.value()));
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(256) k_heston_fused(const __grid_constant__ Pa
       for (int j = 0; j < ILP; ++j) {
         const float dw2 = fmaf(rho, dw1[j], rho_comp * dz[j]);
         const float v_plus = fmaxf(v[j], 0.0f);
-        const float sqrt_v = sqrtf(v_plus);
+        const float sqrt_v = sqrt_approx(v_plus);
         v[j] += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
         lg[j].add(fmaf(nhdt, v_plus, mu_dt) + sqrt_v * sdt * dw1[j]);
       }
@@ -557,7 +557,7 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
         } else {
           const float dw2 = fmaf(rho, dw1, rho_comp * z);
           const float v_plus = fmaxf(v, 0.0f);
-          const float sqrt_v = sqrtf(v_plus);
+          const float sqrt_v = sqrt_approx(v_plus);
           v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
           lg.add(fmaf(nhdt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
           half = false;

@@ -51,8 +51,7 @@ int var_cvar_dev(stocha_ctx* c, const double* returns, uint64_t n, double confid
   if ((rc = begin_call(c))) return rc;
   STOCHA_CUDA(cudaMemcpyAsync(state, c->h_small, sizeof init, cudaMemcpyHostToDevice, c->stream));
   STOCHA_CUDA(cudaMemsetAsync(hist, 0, 256 * 8 + 64, c->stream));
-  launch_check_finite(returns, n, bad, grid, c->stream);
-  launch_select(returns, n, state, hist, grid, c->stream);
+  launch_select(returns, n, state, hist, bad, grid, c->stream);
   launch_tail_sum(returns, n, state, part, grid, c->stream);
   launch_reduce_partials(part, grid, 2, total, c->stream);
   STOCHA_CUDA(cudaGetLastError());

@@ -12,9 +12,9 @@ struct SelectState {
   uint64_t prefix, mask, rank, less, equal;
 };
 
-void launch_check_finite(const double* r, uint64_t n, unsigned* bad, int grid, cudaStream_t st);
-void launch_select(const double* r, uint64_t n, SelectState* state, unsigned long long* hist, int grid,
-                   cudaStream_t st);
+// 8 select passes; the first sets *bad if a return is NaN or infinite.
+void launch_select(const double* r, uint64_t n, SelectState* state, unsigned long long* hist, unsigned* bad,
+                   int grid, cudaStream_t st);
 void launch_tail_sum(const double* r, uint64_t n, const SelectState* state, double* part, int grid, cudaStream_t st);
 
 }  // namespace stocha

@@ -420,9 +420,7 @@ int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, si
   a.tabs = ctx->d_tabs;
   a.err = ctx->d_err;
   a.n = n_samples;
-  // 256 draws (~40 samples at dim 4) per chunk: the emit pass runs one thread
-  // per chunk, so shorter chunks give it enough threads to hide latency
-  a.C = 256;
+  a.C = 1024;
   a.dim = (int)dim;
   // A sample takes dim + 2 draws plus a few on rejections, so the true entry
   // of a chunk (the overshoot of the sample that straddles its start) lies

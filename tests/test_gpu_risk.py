@@ -41,3 +41,10 @@ def test_var_cvar_reference_expectations(stocha):
         stocha.var_cvar(np.array([0.01, np.nan, 0.02]), 0.95)
     with pytest.raises(ValueError, match="returns must not contain NaN or Inf"):
         stocha.var_cvar(np.array([0.01, -np.inf]), 0.95)
+    # one non-finite value at the end of a large array (the check runs inside
+    # the first radix pass, spread over the whole grid)
+    big = np.random.default_rng(1).standard_normal(3_000_001) * 0.02
+    for bad in (np.nan, np.inf, -np.inf):
+        big[-1] = bad
+        with pytest.raises(ValueError, match="returns must not contain NaN or Inf"):
+            stocha.var_cvar(big, 0.99)
