@@ -8,9 +8,12 @@
 //   Heston log S_k += (mu - v+/2) dt + sqrt(v+ dt) dw1   (v in FP32)
 // which equal the reference's products of exponentials (gbm.rs:71,
 // multi_gbm.rs:246, jump_diffusion.rs:87, heston.rs:69) in exact arithmetic.
-// Sums over steps are compensated (Kahan); payoff sums over paths are
+// Sums over steps are compensated (Kahan) where each partial sum is stored
+// and plain in the fused forms (see Plain); payoff sums over paths are
 // compensated FP32 per thread and FP64 per block.
 #include <cuda_runtime.h>
+
+#include <type_traits>
 
 #include "engine.h"
 #include "mc_device.cuh"
@@ -29,6 +32,21 @@ struct Kahan {
   }
   __device__ __forceinline__ float value() const { return s - c; }
 };
+
+// Plain FP32 running sum, for the per-path sums of the fused forms: over 252
+// steps its rounding error (~sqrt(steps) * ulp(sqrt(steps)) / 3.5, about 5e-6
+// absolute for a sum of normals) is of the order of the FP32 normals' own
+// error, so compensation (3 more adds per term) buys nothing there.
+struct Plain {
+  float s = 0.0f;
+  __device__ __forceinline__ void add(float v) { s += v; }
+  __device__ __forceinline__ float value() const { return s; }
+};
+
+// Per-path running sum: compensated where every partial sum is stored (the
+// materialised paths), plain where only the last one is used.
+template <bool kStore>
+using PathSum = typename std::conditional<kStore, Kahan, Plain>::type;
 
 __device__ __forceinline__ float payoff_f32(float s, float k, int kind) {
   return kind == kCall ? fmaxf(s - k, 0.0f) : fmaxf(k - s, 0.0f);
@@ -56,7 +74,7 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
-    Kahan w;
+    PathSum<kStore> w;
     float kf = 0.0f;  // step count as float (no per-step integer conversion)
     if (kStore) store32(a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
@@ -96,7 +114,7 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
-    Kahan w[CAP];
+    PathSum<kStore> w[CAP];
     const F32K& f = a.f32;
     float kf = 0.0f;
     if (kStore)
@@ -156,7 +174,7 @@ __global__ void __launch_bounds__(256) k_heston_euler_f32(const __grid_constant_
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     float v = (float)h.v0;
-    Kahan lg;
+    PathSum<kStore> lg;
     if (kStore) store32(a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
@@ -193,7 +211,7 @@ __global__ void __launch_bounds__(256) k_merton_f32(const __grid_constant__ Path
   for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
-    Kahan w;
+    PathSum<kStore> w;
     float jumps = 0.0f, kf = 0.0f;
     if (kStore) store32(a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
@@ -271,7 +289,7 @@ __global__ void __launch_bounds__(256) k_gbm_fused(const __grid_constant__ PathL
   for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
     bool ok[ILP], neg[ILP];
     PcgGen s[ILP];
-    Kahan w[ILP];
+    Plain w[ILP];
     group_rows<ILP>(a, l0, nthreads, ok, neg, s);
 #pragma unroll 1
     for (uint64_t k = 0; k < a.steps; ++k) {
@@ -306,7 +324,7 @@ __global__ void __launch_bounds__(256) k_heston_fused(const __grid_constant__ Pa
   for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
     bool ok[ILP], neg[ILP];
     PcgGen s[ILP];
-    Kahan lg[ILP];
+    Plain lg[ILP];
     float v[ILP];
     group_rows<ILP>(a, l0, nthreads, ok, neg, s);
 #pragma unroll
@@ -351,7 +369,7 @@ __global__ void __launch_bounds__(256) k_merton_fused(const __grid_constant__ Pa
   for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
     bool ok[ILP], neg[ILP];
     PcgGen s[ILP];
-    Kahan w[ILP];
+    Plain w[ILP];
     float jumps[ILP];
     group_rows<ILP>(a, l0, nthreads, ok, neg, s);
 #pragma unroll
@@ -390,7 +408,7 @@ __global__ void __launch_bounds__(256) k_multi_fused(const __grid_constant__ Pat
   for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
     bool ok[ILP], neg[ILP];
     PcgGen s[ILP];
-    Kahan w[ILP][NA];
+    Plain w[ILP][NA];
     group_rows<ILP>(a, l0, nthreads, ok, neg, s);
 #pragma unroll 1
     for (uint64_t k = 0; k < a.steps; ++k) {
@@ -485,7 +503,7 @@ __global__ void __launch_bounds__(256) k_gbm_uf(const __grid_constant__ PathLaun
   const uint32_t need_all = (uint32_t)a.steps * N, cap = uf_cap(need_all);
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
     WarpRow r = warp_row(a, base);
-    Kahan w[N];
+    Plain w[N];
     ZigLane q;
     const uint32_t need = r.ok ? need_all : 0;
     uint32_t cnt = 0;
@@ -495,7 +513,7 @@ __global__ void __launch_bounds__(256) k_gbm_uf(const __grid_constant__ PathLaun
         w[0].add(z);  // the antithetic sign is applied to the sums
         ++cnt;
         if constexpr (N > 1) {
-          const Kahan t = w[0];
+          const Plain t = w[0];
 #pragma unroll
           for (int i = 0; i + 1 < N; ++i) w[i] = w[i + 1];
           w[N - 1] = t;
@@ -543,7 +561,7 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
     WarpRow r = warp_row(a, base);
     ZigLane q;
-    Kahan lg;
+    Plain lg;
     float v = f.h_v0, dw1 = 0.0f;
     bool half = false;
     const uint32_t need = r.ok ? (uint32_t)a.steps : 0;
@@ -592,7 +610,7 @@ __global__ void __launch_bounds__(256) k_merton_uf(const __grid_constant__ PathL
   for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
     WarpRow r = warp_row(a, base);
     ZigLane q;
-    Kahan w;
+    Plain w;
     float jumps = 0.0f;
     bool in_jump = false;
     const uint32_t need = r.ok ? (uint32_t)a.steps : 0;
