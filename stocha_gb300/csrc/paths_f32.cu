@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
 }
 
 template <int NA, bool kStore>
-__global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, 5) k_multi_gbm_f32(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(256) k_multi_gbm_f32(const __grid_constant__ P
 }
 
 template <bool kStore>
-__global__ void __launch_bounds__(256) k_heston_euler_f32(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, 5) k_heston_euler_f32(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};

@@ -3,8 +3,9 @@
 * FP64 fused price equals exp(-rT) * mean(payoff(S_T)) of the oracle's own
   paths (the reference workflow, greeks.rs:313-320) to FP64_PRICE_RTOL: only
   the summation order differs.
-* FP32 fused price is within FP32_PRICE_RTOL of the FP64 price (the north-star
-  bar is 1e-4; the samplers consume the same draws, so the gap is rounding).
+* FP32 fused price is within FP32_PRICE_RTOL of the FP64 price (the target
+  accuracy of the FP32 forms is 1e-4 relative; the samplers consume the same
+  draws, so the gap is rounding).
 """
 import math
 
