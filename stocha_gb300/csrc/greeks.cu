@@ -223,7 +223,10 @@ __device__ __forceinline__ uint32_t inst_of_item(const GreeksLaunch& g, unsigned
 // A block serves items: the next from the queue counter (persistent grid) or
 // item blockIdx.x (direct: one block per item, so blocks retire after one
 // chunk and work on higher-priority streams gets SMs between them).
-__global__ void __launch_bounds__(256) k_greeks(const GreeksLaunch g) {
+// 3 resident blocks per SM (80 registers instead of 124): the kernel is
+// issue-bound like the fused pricing kernels, and the extra warps hide more
+// of the generator's latency (512-instance batch 90 -> 84 ms on GB300).
+__global__ void __launch_bounds__(256, 3) k_greeks(const GreeksLaunch g) {
   __shared__ ZigShared zs;
   __shared__ unsigned long long item_s;
   zig_stage(zs, g.tabs, false);

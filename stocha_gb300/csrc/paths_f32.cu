@@ -43,6 +43,16 @@ struct Plain {
   __device__ __forceinline__ float value() const { return s; }
 };
 
+// Resident 256-thread blocks per SM the fused kernels are compiled for (a
+// register cap of 48).  These kernels are issue-bound: 5 blocks (40 warps)
+// instead of the 4 that 64 registers allow hide more of the generator's
+// dependent-issue latency, and the values the cap spills belong to the rare
+// wedge and tail paths (measured on GB300: multi-GBM 2.97 -> 2.74 ms, Heston
+// 2.08 -> 2.02 ms, Merton 1.52 -> 1.48 ms; 6 blocks spilled into the common
+// path).  The warp-uniform multi-asset form carries more state: 4 blocks.
+constexpr int kFusedMinBlocks = 5;
+constexpr int kUfMinBlocks = 4;
+
 // Per-path running sum: compensated where every partial sum is stored (the
 // materialised paths), plain where only the last one is used.
 template <bool kStore>
@@ -101,7 +111,7 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
 }
 
 template <int NA, bool kStore>
-__global__ void __launch_bounds__(256, 5) k_multi_gbm_f32(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm_f32(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -159,7 +169,7 @@ __global__ void __launch_bounds__(256, 5) k_multi_gbm_f32(const __grid_constant_
 }
 
 template <bool kStore>
-__global__ void __launch_bounds__(256, 5) k_heston_euler_f32(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_euler_f32(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -198,7 +208,7 @@ __global__ void __launch_bounds__(256, 5) k_heston_euler_f32(const __grid_consta
 }
 
 template <bool kStore>
-__global__ void __launch_bounds__(256) k_merton_f32(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_merton_f32(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -278,7 +288,7 @@ __device__ __forceinline__ void store_partials(const PathLaunch& a, const Kahan*
 }
 
 template <int ILP>
-__global__ void __launch_bounds__(256) k_gbm_fused(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_gbm_fused(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -311,7 +321,7 @@ __global__ void __launch_bounds__(256) k_gbm_fused(const __grid_constant__ PathL
 }
 
 template <int ILP>
-__global__ void __launch_bounds__(256) k_heston_fused(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_heston_fused(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -356,7 +366,7 @@ __global__ void __launch_bounds__(256) k_heston_fused(const __grid_constant__ Pa
 }
 
 template <int ILP>
-__global__ void __launch_bounds__(256) k_merton_fused(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_merton_fused(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -397,7 +407,7 @@ __global__ void __launch_bounds__(256) k_merton_fused(const __grid_constant__ Pa
 }
 
 template <int NA, int ILP>
-__global__ void __launch_bounds__(256) k_multi_fused(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_multi_fused(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -491,7 +501,7 @@ __device__ __forceinline__ void uf_drive(const uint32_t& cnt, uint32_t need, uin
 // normals matter.  The sum being filled is always w[0]; after each normal the
 // sums rotate, so after steps * NA normals they are back in asset order.
 template <int NA>
-__global__ void __launch_bounds__(256) k_gbm_uf(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, kUfMinBlocks) k_gbm_uf(const __grid_constant__ PathLaunch a) {
   constexpr int N = NA > 0 ? NA : 1;
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
@@ -596,7 +606,7 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
 // Merton: after the diffusion normal of a step the lane takes the jump
 // uniform at once (a second generator step in the same iteration); on a jump
 // its next normal is the jump size.
-__global__ void __launch_bounds__(256) k_merton_uf(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(256, kFusedMinBlocks) k_merton_uf(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
