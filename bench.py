@@ -25,10 +25,11 @@ One "step" = one pass of all three models.  Path-steps per step = 3 * 2.52e8
           at 2000/s, through stocha_gb300.Server (40 GB budget): p50/p99
           latency overall and for requests of <= 1e5 paths, requests/s, and
           the per-request error of a sample against the FP64 plain form.
-  exotics_mc, rates_copulas_risk  barrier / Asian / lookback Monte Carlo,
-          Hull-White paths, Gaussian and Student-t copulas and VaR/CVaR
-          through the public API (host arrays), each beside the oracle on a
-          bounded sample.
+  exotics_mc, rates_copulas_risk, api_rows  barrier / Asian / lookback
+          Monte Carlo, Hull-White paths, Gaussian and Student-t copulas,
+          VaR/CVaR, the RNG class, greeks_fd and greeks_pathwise through the
+          public API (host arrays), each beside the oracle on a bounded
+          sample.
 
 --impl reference runs the C++ oracle (the reference itself is Rust and cannot
 be built here) on all host cores for the same workload, each step a sample of
@@ -288,136 +289,189 @@ def bench_serving(stocha, n=20_000, rate=2000.0, budget=40 << 30, lanes=32, samp
 
 
 def bench_extras(stocha, torch, cores, skip_cpu):
-    """Configurations 1, 3 and 4 beside the headline (each a few seconds)."""
+    """The other configurations and rows beside the headline (each a few
+    seconds).  A section that fails records its error instead of ending the
+    run, so the headline line is always printed."""
     import numpy as np
 
     from oracle import oracle as O
 
     res = {}
-    # -- config 1: GBM FP64, 1e5 x 252, seed 42 (the reference's own benchmark case)
-    steps1, n1 = 252, 100_000
-    m = stocha.model_struct("gbm", dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0), steps1, n1)
-    from stocha_gb300 import _lib
 
-    lib = _lib.load()
-    buf = torch.empty((n1, steps1 + 1), dtype=torch.float64, device="cuda")
-    for _ in range(3):
-        _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), 42, _lib.FP64, ctypes.c_void_p(buf.data_ptr())))
-    _lib.check(lib.stocha_ctx_sync(None))
-    k = 20
-    t0 = time.perf_counter()
-    for _ in range(k):
-        _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), 42, _lib.FP64, ctypes.c_void_p(buf.data_ptr())))
-    _lib.check(lib.stocha_ctx_sync(None))
-    dev_s = (time.perf_counter() - t0) / k
-    stocha.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42)
-    t0 = time.perf_counter()
-    for _ in range(5):
-        stocha.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42)
-    e2e_s = (time.perf_counter() - t0) / 5
-    c1 = {"workload": "gbm fp64 1e5 paths x 252 steps, seed 42", "value": n1 * steps1 / dev_s,
-          "unit": "path-steps/s", "e2e": {"value": n1 * steps1 / e2e_s, "unit": "path-steps/s",
-                                          "d2h_bytes_per_step": n1 * (steps1 + 1) * 8}}
-    if not skip_cpu:
-        O.gbm(100.0, 0.05, 0.2, 1.0, steps1, 20_000, seed=42, threads=cores, gather=True)
-        t0 = time.perf_counter()
-        O.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42, threads=cores, gather=True)
-        c1["cpu_baseline"] = {"value": n1 * steps1 / (time.perf_counter() - t0), "cores": cores, "kind": "port"}
-    res["config1_gbm_fp64"] = c1
-    del buf
-    # -- config 3: LSMC American put, s0=k=100, r=.05, sigma=.2, t=1, 50 steps, degree 3
-    c3 = {"workload": "lsmc put s0=k=100 r=.05 sigma=.2 t=1 steps=50 deg=3 seed=42"}
-    for n in (50_000, 4_000_000):
-        row = {}
-        for prec in ("fp64", "fp32"):
-            stocha.lsmc_american_option(100.0, 100.0, 0.05, 0.2, 1.0, 50, n, precision=prec)
-            t0 = time.perf_counter()
-            reps = 5 if n < 1e6 else 3
-            for _ in range(reps):
-                p, se = stocha.lsmc_american_option(100.0, 100.0, 0.05, 0.2, 1.0, 50, n, precision=prec)
-            row[prec] = {"price": p, "std_err": se, "ms": 1e3 * (time.perf_counter() - t0) / reps,
-                         "path_steps_per_s": n * 50 / ((time.perf_counter() - t0) / reps)}
-        row["fp32_minus_fp64"] = row["fp32"]["price"] - row["fp64"]["price"]
-        c3[str(n)] = row
-    if not skip_cpu:
-        t0 = time.perf_counter()
-        p, se = O.lsmc(100.0, 100.0, 0.05, 0.2, 1.0, 50, 50_000, seed=42, threads=cores)
-        c3["cpu_baseline_50000"] = {"price": p, "std_err": se, "ms": 1e3 * (time.perf_counter() - t0),
-                                    "cores": cores, "kind": "port",
-                                    "note": "paths on all cores, backward sweep single-threaded as in lsmc.rs"}
-        c3["50000"]["fp64_minus_cpu_qr"] = c3["50000"]["fp64"]["price"] - p
-    res["config3_lsmc"] = c3
-    # -- config 4: 512 Greeks instances, one persistent FP32 launch
-    insts = greeks_instances()
-    draw_steps = sum(d["n_paths"] * d["steps"] for d in insts)
-    stocha.greeks_batch(insts[:8])
-    t0 = time.perf_counter()
-    g32 = stocha.greeks_batch(insts, precision="fp32")
-    dt = time.perf_counter() - t0
-    sample = list(range(0, 512, 32))
-    g64 = stocha.greeks_batch([insts[i] for i in sample], precision="fp64")
-    rel = np.abs(g32[sample][:, [0, 2, 3, 4, 5, 6]] - g64[:, [0, 2, 3, 4, 5, 6]]) / np.maximum(
-        np.abs(g64[:, [0, 2, 3, 4, 5, 6]]), 1e-3)
-    names = ["price", "delta", "gamma", "vega", "theta", "rho"]
-    res["config4_greeks_batch"] = {
-        "instances": 512, "seconds": dt, "draw_steps": draw_steps,
-        "scenario_path_steps_per_s": 7 * draw_steps / dt, "draw_steps_per_s": draw_steps / dt,
-        "fp32_vs_fp64_rel_err_median": dict(zip(names, np.median(rel, axis=0).tolist())),
-        "fp32_vs_fp64_rel_err_max": dict(zip(names, np.max(rel, axis=0).tolist())),
-        "fp64_sample": f"{len(sample)} instances (every 32nd) revalued scenario by scenario in FP64"}
-    # -- exotic Monte Carlo (barrier / Asian / lookback), FP64, 1e6 x 252
-    ex = {"workload": "1e6 paths x 252 steps, s=k=100 r=.05 sigma=.2 t=1, FP64 Monte Carlo (reference arithmetic)"}
-    cases = [("barrier_uo_call_h120", lambda n: stocha.barrier_price(100, 100, .05, .2, 1., 120, method="mc",
-                                                                     n_paths=n, n_steps=252),
-              lambda n: O.barrier_mc(100, 100, .05, .2, 1., 120, n_paths=n, n_steps=252, threads=cores)),
-             ("asian_arith_fixed_call_cv", lambda n: stocha.asian_price(100, 100, .05, .2, 1., method="mc", n_paths=n),
-              None),
-             ("lookback_floating_call", lambda n: stocha.lookback_price(100, .05, .2, 1., method="mc", n_paths=n),
-              lambda n: O.lookback_mc(100, .05, .2, 1., n_paths=n, threads=cores))]
-    for name, gpu, cpu in cases:
-        gpu(10_000)
-        t0 = time.perf_counter()
-        price = gpu(1_000_000)
-        dt = time.perf_counter() - t0
-        row = {"price": price, "ms": dt * 1e3, "path_steps_per_s": 1e6 * 252 / dt}
-        if cpu is not None and not skip_cpu:
-            t0 = time.perf_counter()
-            cpu(50_000)
-            row["cpu_path_steps_per_s"] = 5e4 * 252 / (time.perf_counter() - t0)
-            row["cpu_cores"] = cores
-        ex[name] = row
-    res["exotics_mc"] = ex
-    # -- Hull-White paths, copulas, VaR / CVaR (host arrays in and out, as the API returns them)
-    rr = {}
-    corr4 = np.full((4, 4), 0.4) + 0.6 * np.eye(4)
-    returns = np.random.default_rng(7).standard_normal(10_000_000) * 0.02
-    cases = [("hull_white_1e5x252", 1e5 * 252, "path-steps/s",
-              lambda: stocha.hull_white(0.05, 0.1, 0.005, 0.01, 1.0, 252, 100_000),
-              lambda: O.hull_white(0.05, 0.1, 0.005, 0.01, 1.0, 252, 100_000, threads=cores), 1e5 * 252),
-             ("gaussian_copula_1e6x4", 1e6, "samples/s", lambda: stocha.gaussian_copula(corr4, 1_000_000),
-              lambda: O.gaussian_copula(corr4, 100_000), 1e5),
-             ("student_t_copula_1e6x4_nu5", 1e6, "samples/s", lambda: stocha.student_t_copula(corr4, 5.0, 1_000_000),
-              lambda: O.student_t_copula(corr4, 5.0, 100_000), 1e5),
-             ("var_cvar_1e7_returns", 1e7, "returns/s", lambda: stocha.var_cvar(returns, 0.99),
-              lambda: O.var_cvar(returns[:1_000_000], 0.99), 1e6)]
-    for name, units, unit, gpu, cpu, cpu_units in cases:
-        gpu()
-        t0 = time.perf_counter()
+    # -- config 1: GBM FP64, 1e5 x 252, seed 42 (the reference's own benchmark case)
+    def _section0():
+        steps1, n1 = 252, 100_000
+        m = stocha.model_struct("gbm", dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0), steps1, n1)
+        from stocha_gb300 import _lib
+
+        lib = _lib.load()
+        buf = torch.empty((n1, steps1 + 1), dtype=torch.float64, device="cuda")
         for _ in range(3):
-            gpu()
-        dt = (time.perf_counter() - t0) / 3
-        row = {"e2e_value": units / dt, "unit": unit, "ms": dt * 1e3}
+            _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), 42, _lib.FP64, ctypes.c_void_p(buf.data_ptr())))
+        _lib.check(lib.stocha_ctx_sync(None))
+        k = 20
+        t0 = time.perf_counter()
+        for _ in range(k):
+            _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), 42, _lib.FP64, ctypes.c_void_p(buf.data_ptr())))
+        _lib.check(lib.stocha_ctx_sync(None))
+        dev_s = (time.perf_counter() - t0) / k
+        stocha.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42)
+        t0 = time.perf_counter()
+        for _ in range(5):
+            stocha.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42)
+        e2e_s = (time.perf_counter() - t0) / 5
+        c1 = {"workload": "gbm fp64 1e5 paths x 252 steps, seed 42", "value": n1 * steps1 / dev_s,
+              "unit": "path-steps/s", "e2e": {"value": n1 * steps1 / e2e_s, "unit": "path-steps/s",
+                                              "d2h_bytes_per_step": n1 * (steps1 + 1) * 8}}
+        if not skip_cpu:
+            O.gbm(100.0, 0.05, 0.2, 1.0, steps1, 20_000, seed=42, threads=cores, gather=True)
+            t0 = time.perf_counter()
+            O.gbm(100.0, 0.05, 0.2, 1.0, steps1, n1, seed=42, threads=cores, gather=True)
+            c1["cpu_baseline"] = {"value": n1 * steps1 / (time.perf_counter() - t0), "cores": cores, "kind": "port"}
+        res["config1_gbm_fp64"] = c1
+        del buf
+
+    # -- config 3: LSMC American put, s0=k=100, r=.05, sigma=.2, t=1, 50 steps, degree 3
+    def _section1():
+        c3 = {"workload": "lsmc put s0=k=100 r=.05 sigma=.2 t=1 steps=50 deg=3 seed=42"}
+        for n in (50_000, 4_000_000):
+            row = {}
+            for prec in ("fp64", "fp32"):
+                stocha.lsmc_american_option(100.0, 100.0, 0.05, 0.2, 1.0, 50, n, precision=prec)
+                t0 = time.perf_counter()
+                reps = 5 if n < 1e6 else 3
+                for _ in range(reps):
+                    p, se = stocha.lsmc_american_option(100.0, 100.0, 0.05, 0.2, 1.0, 50, n, precision=prec)
+                row[prec] = {"price": p, "std_err": se, "ms": 1e3 * (time.perf_counter() - t0) / reps,
+                             "path_steps_per_s": n * 50 / ((time.perf_counter() - t0) / reps)}
+            row["fp32_minus_fp64"] = row["fp32"]["price"] - row["fp64"]["price"]
+            c3[str(n)] = row
         if not skip_cpu:
             t0 = time.perf_counter()
-            cpu()
-            row["cpu_value"] = cpu_units / (time.perf_counter() - t0)
-            # Hull-White paths are per-path parallel (Rayon in the reference); the
-            # copulas are one sequential stream and VaR one sort, single-threaded there
-            row["cpu_cores"] = cores if name.startswith("hull_white") else 1
-        rr[name] = row
-    res["rates_copulas_risk"] = rr
+            p, se = O.lsmc(100.0, 100.0, 0.05, 0.2, 1.0, 50, 50_000, seed=42, threads=cores)
+            c3["cpu_baseline_50000"] = {"price": p, "std_err": se, "ms": 1e3 * (time.perf_counter() - t0),
+                                        "cores": cores, "kind": "port",
+                                        "note": "paths on all cores, backward sweep single-threaded as in lsmc.rs"}
+            c3["50000"]["fp64_minus_cpu_qr"] = c3["50000"]["fp64"]["price"] - p
+        res["config3_lsmc"] = c3
+
+    # -- config 4: 512 Greeks instances, one persistent FP32 launch
+    def _section2():
+        insts = greeks_instances()
+        draw_steps = sum(d["n_paths"] * d["steps"] for d in insts)
+        stocha.greeks_batch(insts[:8])
+        t0 = time.perf_counter()
+        g32 = stocha.greeks_batch(insts, precision="fp32")
+        dt = time.perf_counter() - t0
+        sample = list(range(0, 512, 32))
+        g64 = stocha.greeks_batch([insts[i] for i in sample], precision="fp64")
+        rel = np.abs(g32[sample][:, [0, 2, 3, 4, 5, 6]] - g64[:, [0, 2, 3, 4, 5, 6]]) / np.maximum(
+            np.abs(g64[:, [0, 2, 3, 4, 5, 6]]), 1e-3)
+        names = ["price", "delta", "gamma", "vega", "theta", "rho"]
+        res["config4_greeks_batch"] = {
+            "instances": 512, "seconds": dt, "draw_steps": draw_steps,
+            "scenario_path_steps_per_s": 7 * draw_steps / dt, "draw_steps_per_s": draw_steps / dt,
+            "fp32_vs_fp64_rel_err_median": dict(zip(names, np.median(rel, axis=0).tolist())),
+            "fp32_vs_fp64_rel_err_max": dict(zip(names, np.max(rel, axis=0).tolist())),
+            "fp64_sample": f"{len(sample)} instances (every 32nd) revalued scenario by scenario in FP64"}
+
+    # -- exotic Monte Carlo (barrier / Asian / lookback), FP64, 1e6 x 252
+    def _section3():
+        ex = {"workload": "1e6 paths x 252 steps, s=k=100 r=.05 sigma=.2 t=1, FP64 Monte Carlo (reference arithmetic)"}
+        cases = [("barrier_uo_call_h120", lambda n: stocha.barrier_price(100, 100, .05, .2, 1., 120, method="mc",
+                                                                         n_paths=n, n_steps=252),
+                  lambda n: O.barrier_mc(100, 100, .05, .2, 1., 120, n_paths=n, n_steps=252, threads=cores)),
+                 ("asian_arith_fixed_call_cv", lambda n: stocha.asian_price(100, 100, .05, .2, 1., method="mc", n_paths=n),
+                  None),
+                 ("lookback_floating_call", lambda n: stocha.lookback_price(100, .05, .2, 1., method="mc", n_paths=n),
+                  lambda n: O.lookback_mc(100, .05, .2, 1., n_paths=n, threads=cores))]
+        for name, gpu, cpu in cases:
+            gpu(10_000)
+            t0 = time.perf_counter()
+            price = gpu(1_000_000)
+            dt = time.perf_counter() - t0
+            row = {"price": price, "ms": dt * 1e3, "path_steps_per_s": 1e6 * 252 / dt}
+            if cpu is not None and not skip_cpu:
+                t0 = time.perf_counter()
+                cpu(50_000)
+                row["cpu_path_steps_per_s"] = 5e4 * 252 / (time.perf_counter() - t0)
+                row["cpu_cores"] = cores
+            ex[name] = row
+        res["exotics_mc"] = ex
+
+    # -- Hull-White paths, copulas, VaR / CVaR (host arrays in and out, as the API returns them)
+    def _section4():
+        rr = {}
+        corr4 = np.full((4, 4), 0.4) + 0.6 * np.eye(4)
+        returns = np.random.default_rng(7).standard_normal(10_000_000) * 0.02
+        cases = [("hull_white_1e5x252", 1e5 * 252, "path-steps/s",
+                  lambda: stocha.hull_white(0.05, 0.1, 0.005, 0.01, 1.0, 252, 100_000),
+                  lambda: O.hull_white(0.05, 0.1, 0.005, 0.01, 1.0, 252, 100_000, threads=cores), 1e5 * 252),
+                 ("gaussian_copula_1e6x4", 1e6, "samples/s", lambda: stocha.gaussian_copula(corr4, 1_000_000),
+                  lambda: O.gaussian_copula(corr4, 100_000), 1e5),
+                 ("student_t_copula_1e6x4_nu5", 1e6, "samples/s", lambda: stocha.student_t_copula(corr4, 5.0, 1_000_000),
+                  lambda: O.student_t_copula(corr4, 5.0, 100_000), 1e5),
+                 ("var_cvar_1e7_returns", 1e7, "returns/s", lambda: stocha.var_cvar(returns, 0.99),
+                  lambda: O.var_cvar(returns[:1_000_000], 0.99), 1e6)]
+        for name, units, unit, gpu, cpu, cpu_units in cases:
+            gpu()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                gpu()
+            dt = (time.perf_counter() - t0) / 3
+            row = {"e2e_value": units / dt, "unit": unit, "ms": dt * 1e3}
+            if not skip_cpu:
+                t0 = time.perf_counter()
+                cpu()
+                row["cpu_value"] = cpu_units / (time.perf_counter() - t0)
+                # Hull-White paths are per-path parallel (Rayon in the reference); the
+                # copulas are one sequential stream and VaR one sort, single-threaded there
+                row["cpu_cores"] = cores if name.startswith("hull_white") else 1
+            rr[name] = row
+        res["rates_copulas_risk"] = rr
+
+    # -- the rest of the reference API on the path: RNG class, greeks_fd (FP64), greeks_pathwise
+    def _section5():
+        api = {}
+        gbm_p = dict(s0=100.0, r=0.05, sigma=0.2, t=1.0)
+        five = ["delta", "gamma", "vega", "theta", "rho"]
+        st0, inc0 = O.pcg_seed(42)
+        cases = [("rng_standard_normal_1e7", 1e7, "normals/s", lambda: stocha.RNG(seed=42).standard_normal(10_000_000),
+                  lambda: O.stream_fill(st0, inc0, "standard_normal", 1_000_000), 1e6, 1),
+                 ("rng_uniform_1e7", 1e7, "uniforms/s", lambda: stocha.RNG(seed=42).uniform(10_000_000),
+                  lambda: O.stream_fill(st0, inc0, "uniform", 1_000_000), 1e6, 1),
+                 ("greeks_fd_gbm_5greeks_1e5x252_fp64", 1e5 * 252, "path-steps/s (7 scenarios each)",
+                  lambda: stocha.greeks_fd("gbm", gbm_p, "call", 100.0, 100_000, 252, five),
+                  lambda: O.greeks_fd("gbm", gbm_p, "call", 100.0, 100_000, 252, five, threads=cores), 1e5 * 252, cores),
+                 ("greeks_pathwise_gbm_1e6x252", 1e6 * 252, "path-steps/s",
+                  lambda: stocha.greeks_pathwise(100.0, 0.05, 0.2, 1.0, 100.0, True, 1_000_000, 252, ["delta", "vega"]),
+                  lambda: O.greeks_pathwise(100.0, 0.05, 0.2, 1.0, 100.0, True, 100_000, 252, ["delta", "vega"],
+                                            threads=cores), 1e5 * 252, cores)]
+        for name, units, unit, gpu, cpu, cpu_units, cpu_cores in cases:
+            gpu()
+            t0 = time.perf_counter()
+            for _ in range(3):
+                gpu()
+            dt = (time.perf_counter() - t0) / 3
+            row = {"e2e_value": units / dt, "unit": unit, "ms": dt * 1e3}
+            if not skip_cpu:
+                t0 = time.perf_counter()
+                cpu()
+                row["cpu_value"] = cpu_units / (time.perf_counter() - t0)
+                row["cpu_cores"] = cpu_cores
+            api[name] = row
+        res["api_rows"] = api
+
     # -- config 5: the serving loop
-    res["config5_serving"] = bench_serving(stocha)
+    def _section6():
+        res["config5_serving"] = bench_serving(stocha)
+
+    for fn in (_section0, _section1, _section2, _section3, _section4, _section5, _section6,):
+        try:
+            fn()
+        except Exception as e:  # keep the headline line; record what failed
+            res.setdefault("errors", []).append(f"{fn.__name__}: {e!r}")
+            log(f"bench extras: {fn.__name__} failed: {e!r}")
     return res
 
 

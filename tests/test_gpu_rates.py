@@ -66,7 +66,10 @@ def _corr(dim, seed):
 
 
 @pytest.mark.parametrize("dim,nu,n", [(1, 3.0, 1), (2, 5.0, 1000), (3, 4.5, 100_001), (8, 30.0, 5000),
-                                      (40, 2.5, 2000)])
+                                      (40, 2.5, 2000),
+                                      # shape ~1: frequent gamma rejections, so long samples that
+                                      # straddle a chunk start beyond the dim + 8 candidate entries
+                                      (1, 2.05, 2_000_000)])
 def test_student_t_copula_matches_oracle(stocha, oracle, dim, nu, n):
     """One sequential stream with a variable draw count per sample (Marsaglia-
     Tsang rejection), parsed speculatively on the device: every accept/reject
