@@ -38,7 +38,7 @@ struct ZigTables {
   double r;
   float r32;
   float pad_;
-  double exp2tab[128];  // 2^(j/128) of the table-driven exponential
+  double exp2tab[256];  // 2^(j/256) of the table-driven exponential
 };
 
 // Device error bits (ORed into a per-context word).

@@ -163,8 +163,8 @@ def test_config2_prefix_rows_full_size(stocha, oracle):
 
 
 def test_table_exp_accuracy(stocha):
-    """The FP64 path kernels' exponential (table-driven, 2^(j/128) table plus
-    a degree-5 polynomial) against numpy's exp: <= 3 ulp over the working
+    """The FP64 path kernels' exponential (table-driven, 2^(j/256) table plus
+    a degree-4 polynomial) against numpy's exp: <= 3 ulp over the working
     range, exact special values, subnormal and overflow results."""
     import ctypes
 
