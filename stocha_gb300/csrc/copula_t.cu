@@ -9,14 +9,15 @@
 // at once (k_tparse: samples starting in the chunk, and where the last one
 // ends).  The true entries are then chained through groups of chunks
 // (k_tcompose, k_ttop, k_tfill; a chunk whose entry lies beyond the
-// candidates is parsed where it is met),
-// k_temit re-parses every chunk from its true entry and stores each sample's
-// chi-square and normals, and k_tcdf forms the uniforms
-// u = T_nu((L z)_j * sqrt(nu / chi2)) with the reference's Student-t CDF
-// (regularized incomplete beta by the modified-Lentz continued fraction,
-// Lanczos log-gamma formed on the host; student_t.rs:6-91).  Every decision uses the
-// reference's FP64 values (exact normals; ln in the gamma test and the CDF
-// from the device libm).
+// candidates is parsed where it is met), k_temit re-parses every chunk from
+// its true entry and stores each sample's chi-square and normals, and k_tcdf
+// forms the uniforms u = T_nu((L z)_j * sqrt(nu / chi2)) with the
+// reference's Student-t CDF (regularized incomplete beta by the
+// modified-Lentz continued fraction, Lanczos log-gamma formed on the host;
+// student_t.rs:6-91).  Every accept/reject decision uses the reference's FP64
+// values (exact normals; ln in the gamma test from the device libm); the CDF
+// differs from the reference's by rounding only (Newton reciprocals, host
+// coefficients).
 #include <cuda_runtime.h>
 
 #include "copula_t_kernels.h"
@@ -203,23 +204,29 @@ __global__ void __launch_bounds__(128) k_temit(const __grid_constant__ TParse a,
 // Modified Lentz continued fraction of the incomplete beta (student_t.rs:40-72).
 // The even and odd partial numerators are x times coefficients of m alone
 // (cf[2(m-1)], cf[2(m-1)+1]), formed once per call on the host.
+// Each half step needs 1/d' (the new d) and, for the next half step, 1/c:
+// both come from one reciprocal of the product d' c.
 __device__ double beta_cf(double x, double a, double b, const double* __restrict__ cf) {
   const double EPS = 3e-7, FPMIN = 1e-30;
   const double qab = a + b, qap = a + 1.0;
-  double c = 1.0;
+  double c = 1.0, rc = 1.0;  // c and 1/c
   double d = fmax(1.0 - qab * x / qap, FPMIN);
   d = recip_nr(d);
   double h = d;
   for (int m = 1; m <= 200; ++m) {
     double aa = __ldg(cf + 2 * (m - 1)) * x;
-    d = fmax(fabs(1.0 + aa * d), FPMIN);
-    c = fmax(fabs(1.0 + aa * recip_nr(c)), FPMIN);
-    d = recip_nr(d);
+    double dp = fmax(fabs(1.0 + aa * d), FPMIN);
+    c = fmax(fabs(1.0 + aa * rc), FPMIN);
+    double r = recip_nr(dp * c);
+    d = r * c;
+    rc = r * dp;
     h *= d * c;
     aa = __ldg(cf + 2 * (m - 1) + 1) * x;
-    d = fmax(fabs(1.0 + aa * d), FPMIN);
-    c = fmax(fabs(1.0 + aa * recip_nr(c)), FPMIN);
-    d = recip_nr(d);
+    dp = fmax(fabs(1.0 + aa * d), FPMIN);
+    c = fmax(fabs(1.0 + aa * rc), FPMIN);
+    r = recip_nr(dp * c);
+    d = r * c;
+    rc = r * dp;
     const double del = d * c;
     h *= del;
     if (fabs(del - 1.0) < EPS) break;
