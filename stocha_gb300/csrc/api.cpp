@@ -630,6 +630,7 @@ int stocha_tune_set(int32_t model, int32_t n_assets, int32_t block, int32_t ilp,
 }
 
 int stocha_autotune(stocha_ctx* ctx, const stocha_model* m, int32_t reps, stocha_tune_result* out) {
+  STOCHA_RANGE("stocha_autotune");
   if (!m || !out) return set_error(STOCHA_ERR_VALUE, "model and out must not be NULL");
   const int slot = tune_slot_of(m->kind, m->n_assets);
   if (slot < 0 || (m->kind == STOCHA_MODEL_HESTON && m->scheme != 0))
@@ -731,6 +732,7 @@ const char* stocha_version(void) { return "1.7.1"; }
 
 int stocha_gbm(stocha_ctx* ctx, double s0, double mu, double sigma, double t, uint64_t steps, uint64_t n_paths,
                uint64_t seed, int32_t antithetic, double q, double* out) {
+  STOCHA_RANGE("stocha_gbm");
   stocha_model m;
   std::memset(&m, 0, sizeof m);
   m.kind = STOCHA_MODEL_GBM;
@@ -748,6 +750,7 @@ int stocha_gbm(stocha_ctx* ctx, double s0, double mu, double sigma, double t, ui
 int stocha_heston(stocha_ctx* ctx, double s0, double v0, double mu, double kappa, double theta, double xi,
                   double rho, double t, uint64_t steps, uint64_t n_paths, uint64_t seed, const char* scheme,
                   double* out) {
+  STOCHA_RANGE("stocha_heston");
   stocha_model m;
   std::memset(&m, 0, sizeof m);
   m.kind = STOCHA_MODEL_HESTON;
@@ -768,6 +771,7 @@ int stocha_heston(stocha_ctx* ctx, double s0, double v0, double mu, double kappa
 int stocha_merton_jump_diffusion(stocha_ctx* ctx, double s0, double mu, double sigma, double lambda_, double mu_j,
                                  double sigma_j, double t, uint64_t steps, uint64_t n_paths, uint64_t seed,
                                  double* out) {
+  STOCHA_RANGE("stocha_merton_jump_diffusion");
   stocha_model m;
   std::memset(&m, 0, sizeof m);
   m.kind = STOCHA_MODEL_MERTON;
@@ -785,6 +789,7 @@ int stocha_merton_jump_diffusion(stocha_ctx* ctx, double s0, double mu, double s
 
 int stocha_hull_white(stocha_ctx* ctx, double r0, double a, double theta, double sigma, double t, uint64_t steps,
                       uint64_t n_paths, uint64_t seed, double* out) {
+  STOCHA_RANGE("stocha_hull_white");
   stocha_model m;
   std::memset(&m, 0, sizeof m);
   m.kind = STOCHA_MODEL_HULL_WHITE;
@@ -801,6 +806,7 @@ int stocha_hull_white(stocha_ctx* ctx, double r0, double a, double theta, double
 int stocha_multi_gbm(stocha_ctx* ctx, size_t n_assets, const double* s0, const double* mu, const double* sigma,
                      const double* corr, size_t corr_rows, size_t corr_cols, double t, uint64_t steps,
                      uint64_t n_paths, uint64_t seed, int32_t antithetic, double* out) {
+  STOCHA_RANGE("stocha_multi_gbm");
   // lib.rs:771-809: the length checks come first, the corr shape last.
   if (n_assets == 0) return set_error(STOCHA_ERR_VALUE, "s0 must not be empty");
   for (size_t i = 0; i < n_assets; ++i)
@@ -829,6 +835,7 @@ int stocha_multi_gbm(stocha_ctx* ctx, size_t n_assets, const double* s0, const d
 }
 
 int stocha_paths_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, void* out_dev) {
+  STOCHA_RANGE("stocha_paths_device");
   int rc = resolve_ctx(&ctx);
   if (rc) return rc;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
@@ -838,6 +845,7 @@ int stocha_paths_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, i
 
 int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
                         double strike, double rate, double* out_dev) {
+  STOCHA_RANGE("stocha_price_device");
   (void)rate;  // the device form returns raw sums; see stocha_price
   int rc = resolve_ctx(&ctx);
   if (rc) return rc;
@@ -851,6 +859,7 @@ int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, i
 
 int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
                  double strike, double rate, double* out) {
+  STOCHA_RANGE("stocha_price");
   {
     PathLaunch probe;
     uint64_t row_len = 0;

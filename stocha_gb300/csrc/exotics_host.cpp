@@ -483,6 +483,7 @@ int stocha_barrier_price(stocha_ctx* ctx, double s, double k, double r, double s
                          const char* barrier_type, const char* option_type, double q, uint64_t n_paths,
                          uint64_t n_steps, uint64_t seed, const char* method, int32_t n_monitoring, double rebate,
                          int32_t rebate_at_hit, double* price) {
+  STOCHA_RANGE("stocha_barrier_price");
   // lib.rs:1567-1582
   if (s <= 0.0) return set_error(STOCHA_ERR_VALUE, "s must be positive");
   if (k <= 0.0) return set_error(STOCHA_ERR_VALUE, "k must be positive");
@@ -530,6 +531,7 @@ int stocha_asian_price(stocha_ctx* ctx, double s, double k, double r, double sig
                        const char* average_type, const char* strike_type, const char* option_type, double q,
                        uint64_t n_paths, uint64_t seed, const char* method, double running_avg, double time_elapsed,
                        double* price) {
+  STOCHA_RANGE("stocha_asian_price");
   // lib.rs:1664-1716
   if (s <= 0.0) return set_error(STOCHA_ERR_VALUE, "s must be positive");
   if (k <= 0.0) return set_error(STOCHA_ERR_VALUE, "k must be positive");
@@ -584,6 +586,7 @@ int stocha_lookback_price(stocha_ctx* ctx, double s, double r, double sigma, dou
                           const char* strike_type, const char* option_type, double k, double q, uint64_t n_paths,
                           uint64_t seed, const char* method, double running_max, double running_min,
                           double* price) {
+  STOCHA_RANGE("stocha_lookback_price");
   // lib.rs:1779-1814
   if (s <= 0.0) return set_error(STOCHA_ERR_VALUE, "s must be positive");
   if (sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");

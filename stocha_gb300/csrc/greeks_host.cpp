@@ -346,6 +346,7 @@ int stocha_greeks_fd(stocha_ctx* ctx, const char* model, const stocha_greeks_par
                      stocha_payoff_fn payoff_cb, void* user, double strike, uint64_t n_paths, uint64_t n_steps,
                      const char* const* greeks, uint64_t n_greeks, uint64_t seed, double bump_size,
                      int32_t precision, double* out) {
+  STOCHA_RANGE("stocha_greeks_fd");
   std::vector<int> gl;
   int rc = parse_greeks(greeks, n_greeks, &gl);  // lib.rs:1077
   if (rc) return rc;
@@ -379,6 +380,7 @@ int stocha_greeks_fd(stocha_ctx* ctx, const char* model, const stocha_greeks_par
 int stocha_greeks_pathwise(stocha_ctx* ctx, double s0, double r, double sigma, double t, double strike,
                            int32_t is_call, uint64_t n_paths, uint64_t n_steps, const char* const* greeks,
                            uint64_t n_greeks, uint64_t seed, double* out) {
+  STOCHA_RANGE("stocha_greeks_pathwise");
   // lib.rs:1191-1224
   if (s0 <= 0.0) return set_error(STOCHA_ERR_VALUE, "s0 must be positive");
   if (sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
@@ -422,6 +424,7 @@ int stocha_greeks_pathwise(stocha_ctx* ctx, double s0, double r, double sigma, d
 
 int stocha_greeks_batch(stocha_ctx* ctx, const stocha_greeks_instance* inst, uint64_t n, int32_t precision,
                         double* out) {
+  STOCHA_RANGE("stocha_greeks_batch");
   for (uint64_t i = 0; i < n; ++i) {
     const stocha_greeks_instance& x = inst[i];
     if (x.model != STOCHA_MODEL_GBM && x.model != STOCHA_MODEL_HESTON && x.model != STOCHA_MODEL_MERTON)

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <mutex>
 #include <string>
 
@@ -12,6 +14,17 @@
 typedef unsigned __int128 u128;
 
 namespace stocha {
+
+// A named range on the NVTX timeline (Nsight Systems, Nsight Compute) for
+// the duration of one C-ABI call; without an attached tool it costs a
+// pointer test.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define STOCHA_RANGE(name) ::stocha::NvtxRange stocha_nvtx_range_(name)
 
 struct LsmcGraphs;
 

@@ -151,6 +151,7 @@ int stocha_lsmc_american_option(stocha_ctx* ctx, double s0, double k, double r, 
 int stocha_lsmc(stocha_ctx* ctx, double s0, double k, double r, double sigma, double t, uint64_t steps,
                 uint64_t n_paths, int32_t is_put, uint64_t poly_degree, uint64_t seed, int32_t precision,
                 double* price, double* std_err) {
+  STOCHA_RANGE("stocha_lsmc");
   return lsmc_run(ctx, make_job(s0, k, r, sigma, t, steps, n_paths, is_put, poly_degree, seed, precision), price,
                   std_err);
 }

@@ -141,18 +141,6 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
   if (err) atomicOr(a.err, err);
 }
 
-// Rust powi for small non-negative exponents (compiler-rt __powidf2).
-__device__ __forceinline__ double powi_f64(double a, int b) {
-  double r = 1.0;
-  for (;;) {
-    if (b & 1) r *= a;
-    b /= 2;
-    if (b == 0) break;
-    a *= a;
-  }
-  return r;
-}
-
 template <bool kStore>
 __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;

@@ -79,6 +79,7 @@ int var_cvar_dev(stocha_ctx* c, const double* returns, uint64_t n, double confid
 extern "C" {
 
 int stocha_var_cvar(stocha_ctx* ctx, const double* returns, uint64_t n, double confidence, double* out2) {
+  STOCHA_RANGE("stocha_var_cvar");
   int rc = check_args(n, confidence);
   if (rc) return rc;
   if ((rc = resolve_ctx(&ctx))) return rc;
@@ -90,6 +91,7 @@ int stocha_var_cvar(stocha_ctx* ctx, const double* returns, uint64_t n, double c
 }
 
 int stocha_var_cvar_device(stocha_ctx* ctx, const double* returns_dev, uint64_t n, double confidence, double* out2) {
+  STOCHA_RANGE("stocha_var_cvar_device");
   int rc = check_args(n, confidence);
   if (rc) return rc;
   if ((rc = resolve_ctx(&ctx))) return rc;

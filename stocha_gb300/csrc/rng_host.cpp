@@ -287,18 +287,22 @@ const Json::Val* field(const Json::Val& o, const char* k) {
 extern "C" {
 
 int stocha_rng_uniform(stocha_ctx* ctx, stocha_rng* r, uint64_t size, double* out) {
+  STOCHA_RANGE("stocha_rng_uniform");
   return fill_raw(ctx, r, size, 1, out);
 }
 
 int stocha_rng_raw_u64(stocha_ctx* ctx, stocha_rng* r, uint64_t size, uint64_t* out) {
+  STOCHA_RANGE("stocha_rng_raw_u64");
   return fill_raw(ctx, r, size, 0, out);
 }
 
 int stocha_rng_standard_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t size, double* out) {
+  STOCHA_RANGE("stocha_rng_standard_normal");
   return fill_normal(ctx, r, size, 1, 0.0, 1.0, out);
 }
 
 int stocha_rng_normal(stocha_ctx* ctx, stocha_rng* r, uint64_t size, double loc, double scale, double* out) {
+  STOCHA_RANGE("stocha_rng_normal");
   if (scale <= 0.0) return set_error(STOCHA_ERR_VALUE, "scale must be positive");  // lib.rs:137-141
   return fill_normal(ctx, r, size, 2, loc, scale, out);
 }
@@ -339,6 +343,7 @@ int stocha_rng_from_state(const char* json, stocha_rng* out) {
 
 int stocha_gaussian_copula(stocha_ctx* ctx, const double* corr, size_t rows, size_t cols, uint64_t n_samples,
                            uint64_t seed, double* out) {
+  STOCHA_RANGE("stocha_gaussian_copula");
   std::vector<double> l;
   int rc = copula_factor(corr, rows, cols, &l);  // gaussian.rs:21-51
   if (rc) return rc;
@@ -384,6 +389,7 @@ static double lgamma_lanczos(double x) {
 
 int stocha_student_t_copula(stocha_ctx* ctx, const double* corr, size_t rows, size_t cols, double nu,
                             uint64_t n_samples, uint64_t seed, double* out) {
+  STOCHA_RANGE("stocha_student_t_copula");
   if (nu <= 2.0) return set_error(STOCHA_ERR_VALUE, "nu must be > 2");  // lib.rs:570-572 (NaN passes, as there)
   std::vector<double> l;
   if (cols != rows) return set_error(STOCHA_ERR_VALUE, "correlation matrix must be square");  // student_t.rs:146-148
