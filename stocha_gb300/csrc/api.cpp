@@ -510,12 +510,21 @@ int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precis
     return STOCHA_OK;
   }
   const int na = m->kind == STOCHA_MODEL_MULTI_GBM ? m->n_assets : 1;
-  // partial records: at most (SMs * 64) blocks of 2*na doubles
+  // partial records: at most (SMs * 64) blocks of 2*na doubles, or one per
+  // work-queue batch of the FP32 forms (32 rows per batch, more when the
+  // rows would need over 65536 records); the queue counter follows them
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
-  const size_t max_blocks = (size_t)sms * 64 + 1;
-  if ((rc = ensure_buf(c, c->partials, max_blocks * 2 * na * sizeof(double)))) return rc;
+  const uint64_t kMaxBatches = 1ull << 16;
+  const uint64_t per_lane = (L.rows + 32 * kMaxBatches - 1) / (32 * kMaxBatches);
+  L.batch_rows = (uint32_t)(32 * (per_lane ? per_lane : 1));
+  const size_t nbatch = (size_t)((L.rows + L.batch_rows - 1) / L.batch_rows);
+  size_t nrec = (size_t)sms * 64 + 1;
+  if (nbatch > nrec) nrec = nbatch;
+  const size_t rec_bytes = (nrec * 2 * na * sizeof(double) + 255) & ~(size_t)255;
+  if ((rc = ensure_buf(c, c->partials, rec_bytes + 256))) return rc;
   L.partials = (double*)c->partials.ptr;
+  if (precision == STOCHA_FP32) L.work = (unsigned long long*)((char*)c->partials.ptr + rec_bytes);
   int nb = precision == STOCHA_FP32 ? launch_paths_f32(L, c->stream) : launch_paths_f64(L, c->stream);
   if (nb < 0) return cuda_error(cudaGetLastError(), "pricing kernel launch");
   launch_reduce_partials(L.partials, nb, 2 * na, sums_dev, c->stream);

@@ -65,6 +65,11 @@ struct PathLaunch {
   int terminal_only;  // 1: out[row] = S_T only (terminal prices, greeks.rs:165-166)
   // fused mode: per-block partial sums {sum payoff, sum payoff^2} per asset
   double* partials;
+  // fused FP32 mode with a work queue (work != nullptr): warps take batches
+  // of batch_rows consecutive rows (a multiple of 32) from the counter *work,
+  // which the launcher zeroes, and write one partial record per batch
+  unsigned long long* work;
+  uint32_t batch_rows;
   double strike;
   int payoff;
   double aux[4];  // payoff parameters (pathwise estimators: s0, r, sigma, t)
@@ -96,8 +101,9 @@ int set_fused_tune(int slot, FusedTune t);  // 0, or -1 for an invalid slot or s
 // Rounds the FP32 constants of L (after the model constants are set).
 void fill_f32_constants(PathLaunch* L);
 
-// Launch helpers (paths_f64.cu / paths_f32.cu).  Return the number of blocks
-// launched (= number of partial records in fused mode), or -1 on error.
+// Launch helpers (paths_f64.cu / paths_f32.cu).  Return the number of
+// partial records written in fused mode (blocks launched, or batches in the
+// work-queue mode), or -1 on error.
 int launch_paths_f64(const PathLaunch& L, cudaStream_t st);
 int launch_paths_f32(const PathLaunch& L, cudaStream_t st);
 // y[i] = exp(x[i]) by the kernels' table-driven exponential (diagnostic).

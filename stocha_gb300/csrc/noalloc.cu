@@ -42,6 +42,7 @@ constexpr size_t kNoAllocScratch = (size_t)kNoAllocMaxBlocks * 2 * kNoAllocMaxAs
 static __device__ __align__(256) double g_scratch[kNoAllocScratch];
 static __device__ __align__(256) ZigTables g_tables[1];
 static __device__ __align__(256) unsigned g_status[64];
+static __device__ __align__(256) unsigned long long g_work[32];  // work-queue counter of the FP32 forms
 
 constexpr int kMaxDevices = 64;
 struct DeviceArrays {
@@ -49,6 +50,7 @@ struct DeviceArrays {
   double* scratch = nullptr;
   ZigTables* tables = nullptr;
   unsigned* status = nullptr;
+  unsigned long long* work = nullptr;
 };
 std::mutex g_setup_mu;
 DeviceArrays g_dev[kMaxDevices];
@@ -62,6 +64,7 @@ int setup(int dev, DeviceArrays** out) {
     STOCHA_CUDA(cudaGetSymbolAddress((void**)&d.scratch, g_scratch));
     STOCHA_CUDA(cudaGetSymbolAddress((void**)&d.tables, g_tables));
     STOCHA_CUDA(cudaGetSymbolAddress((void**)&d.status, g_status));
+    STOCHA_CUDA(cudaGetSymbolAddress((void**)&d.work, g_work));
     ZigTables host;
     fill_zig_tables(&host);
     STOCHA_CUDA(cudaMemcpyToSymbol(g_tables, &host, sizeof host));
@@ -105,6 +108,13 @@ extern "C" int stocha_price_noalloc(const stocha_model* m, uint64_t seed, int32_
   L.tabs = d->tables;
   L.err = d->status;
   L.partials = d->scratch;
+  if (precision == STOCHA_FP32) {
+    // the FP32 forms' work queue: one record per batch, at most the scratch's
+    // kNoAllocMaxBlocks records (batches of 32 rows, more for large counts)
+    const uint64_t per_lane = (L.rows + 32ull * kNoAllocMaxBlocks - 1) / (32ull * kNoAllocMaxBlocks);
+    L.batch_rows = (uint32_t)(32 * (per_lane ? per_lane : 1));
+    L.work = d->work;
+  }
   L.strike = strike;
   L.payoff = payoff;
   fill_f32_constants(&L);

@@ -70,17 +70,98 @@ __device__ __forceinline__ void store32(const PathLaunch& a, uint64_t lrow, uint
     a.out_f32[(lrow * (a.steps + 1) + step) * width + col] = v;
 }
 
+// Block partial record: {sum payoff, sum payoff^2} per asset, compensated
+// FP32 per thread and FP64 across the block (all threads must call it).
+template <int NV>
+__device__ __forceinline__ void store_partials(const PathLaunch& a, const Kahan* acc, const Kahan* acc2) {
+  float s[2 * NV], c[2 * NV];
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    s[2 * i] = acc[i].s;
+    c[2 * i] = acc[i].c;
+    s[2 * i + 1] = acc2[i].s;
+    c[2 * i + 1] = acc2[i].c;
+  }
+  block_sum_kahan_store<2 * NV>(s, c, a.partials + (uint64_t)blockIdx.x * 2 * NV);
+}
+
+// Row driver of the fused kernels.  batch(b, p) prices row b + lane of a
+// warp's batch of 32 consecutive rows (called by all 32 lanes; it returns
+// false, without simulating, for a row past the end) and leaves the row's
+// payoff per asset in p.
+//   * static (a.work null): warp batches in grid-stride order; one record per
+//     block (store_partials).
+//   * work queue: a warp takes a.batch_rows consecutive rows at a time from
+//     the launch counter *a.work and writes one record per batch, the batch's
+//     sums in a fixed lane order (FP64 warp tree).  Every SM stays busy until
+//     the last batch (a static grid of P paths per thread leaves most SMs idle
+//     through the last round when the rows are not a multiple of the
+//     resident threads), and the records do not depend on which warp ran
+//     which batch, so the price is the same run to run.
+template <int NV, class Batch>
+__device__ __forceinline__ void run_rows(const PathLaunch& a, Batch&& batch) {
+  const unsigned lane = threadIdx.x & 31u;
+  if (a.work) {
+    const uint32_t per_lane = a.batch_rows >> 5;
+#pragma unroll 1
+    for (;;) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(a.work, (unsigned long long)a.batch_rows);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base >= a.rows) break;
+      Kahan s[NV], s2[NV];
+#pragma unroll 1
+      for (uint32_t j = 0; j < per_lane; ++j) {
+        const uint64_t b = base + 32ull * j;
+        if (b >= a.rows) break;  // warp-uniform
+        float p[NV];
+        if (batch(b, p)) {
+#pragma unroll
+          for (int i = 0; i < NV; ++i) {
+            s[i].add(p[i]);
+            s2[i].add(p[i] * p[i]);
+          }
+        }
+      }
+      double* rec = a.partials + (base / a.batch_rows) * (2 * NV);
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        const double v = warp_sum((double)s[i].value());
+        const double v2 = warp_sum((double)s2[i].value());
+        if (lane == 0) {
+          rec[2 * i] = v;
+          rec[2 * i + 1] = v2;
+        }
+      }
+    }
+    return;
+  }
+  Kahan acc[NV], acc2[NV];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+#pragma unroll 1
+  for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); b < a.rows; b += nthreads) {
+    float p[NV];
+    if (batch(b, p)) {
+#pragma unroll
+      for (int i = 0; i < NV; ++i) {
+        acc[i].add(p[i]);
+        acc2[i].add(p[i] * p[i]);
+      }
+    }
+  }
+  store_partials<NV>(a, acc, acc2);
+}
+
 template <bool kStore>
 __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   unsigned err = 0;
-  Kahan acc, acc2;
   const float s0 = (float)a.gbm.s0, drift = (float)a.gbm.drift, diffusion = (float)a.gbm.diffusion;
   const float strike = (float)a.strike;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  // one path: materialised rows (kStore) or the payoff of S_T
+  auto path = [&](uint64_t lrow, float* pay) {
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
@@ -100,13 +181,21 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
     }
     if (!kStore) {
       const float sum = neg ? -w.value() : w.value();
-      float sT = s0 * expf(fmaf(diffusion, sum, a.f32.g_kdrift));
-      float p = payoff_f32(sT, strike, a.payoff);
-      acc.add(p);
-      acc2.add(p * p);
+      pay[0] = payoff_f32(s0 * expf(fmaf(diffusion, sum, a.f32.g_kdrift)), strike, a.payoff);
     }
+  };
+  if constexpr (kStore) {
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads)
+      path(lrow, nullptr);
+  } else {
+    run_rows<1>(a, [&](uint64_t b, float* p) {
+      const uint64_t lrow = b + (threadIdx.x & 31u);
+      if (lrow >= a.rows) return false;
+      path(lrow, p);
+      return true;
+    });
   }
-  if (!kStore) block_sum2_store((double)acc.value(), (double)acc2.value(), a.partials + 2 * blockIdx.x);
   if (err) atomicOr(a.err, err);
 }
 
@@ -118,14 +207,12 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm
   constexpr int CAP = NA > 0 ? NA : kMaxAssets;
   const int na = NA > 0 ? NA : a.multi.na;
   unsigned err = 0;
-  Kahan acc[CAP], acc2[CAP];
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  const F32K& f = a.f32;
+  auto path = [&](uint64_t lrow, float* pay) {
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
     PathSum<kStore> w[CAP];
-    const F32K& f = a.f32;
     float kf = 0.0f;
     if (kStore)
       for (int i = 0; i < na; ++i) store32(a, lrow, 0, na, i, f.a_s0[i]);
@@ -155,16 +242,36 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm
 #pragma unroll
         for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], neg ? -w[m].value() : w[m].value(), eps);
         float lg = fmaf(f.a_diff[i], eps, f.a_kdrift[i]);
-        float p = payoff_f32(f.a_s0[i] * expf(lg), f.strike, a.payoff);
-        acc[i].add(p);
-        acc2[i].add(p * p);
+        pay[i] = payoff_f32(f.a_s0[i] * expf(lg), f.strike, a.payoff);
       }
     }
+  };
+  if constexpr (!kStore && NA > 0) {
+    run_rows<NA>(a, [&](uint64_t b, float* p) {
+      const uint64_t lrow = b + (threadIdx.x & 31u);
+      if (lrow >= a.rows) return false;
+      path(lrow, p);
+      return true;
+    });
+  } else {
+    // materialised rows, or the fused form for more than 4 assets (static,
+    // one record of na assets per block)
+    Kahan acc[CAP], acc2[CAP];
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+      float p[CAP];
+      path(lrow, p);
+      if (!kStore)
+        for (int i = 0; i < na; ++i) {
+          acc[i].add(p[i]);
+          acc2[i].add(p[i] * p[i]);
+        }
+    }
+    if (!kStore)
+      for (int i = 0; i < na; ++i)
+        block_sum2_store((double)acc[i].value(), (double)acc2[i].value(),
+                         a.partials + (2 * (uint64_t)blockIdx.x) * na + 2 * i);
   }
-  if (!kStore)
-    for (int i = 0; i < na; ++i)
-      block_sum2_store((double)acc[i].value(), (double)acc2[i].value(),
-                       a.partials + (2 * (uint64_t)blockIdx.x) * na + 2 * i);
   if (err) atomicOr(a.err, err);
 }
 
@@ -178,9 +285,7 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_eu
   const float theta = (float)h.theta, xi_sdt = (float)(h.xi * h.sqrt_dt), sdt = (float)h.sqrt_dt;
   const float mu_dt = (float)(h.mu * h.dt), half_dt = (float)(0.5 * h.dt), s0 = (float)h.s0;
   unsigned err = 0;
-  Kahan acc, acc2;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  auto path = [&](uint64_t lrow, float* pay) {
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     float v = (float)h.v0;
@@ -197,13 +302,20 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_eu
       lg.add(fmaf(-half_dt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
       if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(lg.value()));
     }
-    if (!kStore) {
-      float p = payoff_f32(s0 * expf(lg.value()), a.f32.strike, a.payoff);
-      acc.add(p);
-      acc2.add(p * p);
-    }
+    if (!kStore) pay[0] = payoff_f32(s0 * expf(lg.value()), a.f32.strike, a.payoff);
+  };
+  if constexpr (kStore) {
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads)
+      path(lrow, nullptr);
+  } else {
+    run_rows<1>(a, [&](uint64_t b, float* p) {
+      const uint64_t lrow = b + (threadIdx.x & 31u);
+      if (lrow >= a.rows) return false;
+      path(lrow, p);
+      return true;
+    });
   }
-  if (!kStore) block_sum2_store((double)acc.value(), (double)acc2.value(), a.partials + 2 * blockIdx.x);
   if (err) atomicOr(a.err, err);
 }
 
@@ -216,9 +328,7 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_merton_f3
   const float drift = (float)M.drift, diffusion = (float)M.diffusion, mu_j = (float)M.mu_j;
   const float sigma_j = (float)M.sigma_j, s0 = (float)M.s0;
   unsigned err = 0;
-  Kahan acc, acc2;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  auto path = [&](uint64_t lrow, float* pay) {
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     PathSum<kStore> w;
@@ -232,14 +342,21 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_merton_f3
       kf += 1.0f;
       if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value()) + jumps));
     }
-    if (!kStore) {
-      float sT = s0 * expf(fmaf(diffusion, w.value(), a.f32.m_kdrift) + jumps);
-      float p = payoff_f32(sT, a.f32.strike, a.payoff);
-      acc.add(p);
-      acc2.add(p * p);
-    }
+    if (!kStore)
+      pay[0] = payoff_f32(s0 * expf(fmaf(diffusion, w.value(), a.f32.m_kdrift) + jumps), a.f32.strike, a.payoff);
+  };
+  if constexpr (kStore) {
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads)
+      path(lrow, nullptr);
+  } else {
+    run_rows<1>(a, [&](uint64_t b, float* p) {
+      const uint64_t lrow = b + (threadIdx.x & 31u);
+      if (lrow >= a.rows) return false;
+      path(lrow, p);
+      return true;
+    });
   }
-  if (!kStore) block_sum2_store((double)acc.value(), (double)acc2.value(), a.partials + 2 * blockIdx.x);
   if (err) atomicOr(a.err, err);
 }
 
@@ -272,19 +389,6 @@ __device__ __forceinline__ void group_rows(const PathLaunch& a, uint64_t l0, uin
     neg[j] = row >= a.base_paths;
     s[j] = PcgGen{pcg_path_state(a.ss, neg[j] ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
   }
-}
-
-template <int NV>
-__device__ __forceinline__ void store_partials(const PathLaunch& a, const Kahan* acc, const Kahan* acc2) {
-  float s[2 * NV], c[2 * NV];
-#pragma unroll
-  for (int i = 0; i < NV; ++i) {
-    s[2 * i] = acc[i].s;
-    c[2 * i] = acc[i].c;
-    s[2 * i + 1] = acc2[i].s;
-    c[2 * i + 1] = acc2[i].c;
-  }
-  block_sum_kahan_store<2 * NV>(s, c, a.partials + (uint64_t)blockIdx.x * 2 * NV);
 }
 
 template <int ILP>
@@ -508,10 +612,8 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_gbm_uf(const __grid_const
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const F32K& f = a.f32;
   unsigned err = 0;
-  Kahan acc[N], acc2[N];
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
   const uint32_t need_all = (uint32_t)a.steps * N, cap = uf_cap(need_all);
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
+  run_rows<N>(a, [&](uint64_t base, float* pay) {
     WarpRow r = warp_row(a, base);
     Plain w[N];
     ZigLane q;
@@ -546,13 +648,11 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_gbm_uf(const __grid_const
           lg = fmaf(f.a_diff[i], eps, f.a_kdrift[i]);
           s0 = f.a_s0[i];
         }
-        const float p = payoff_f32(s0 * expf(lg), f.strike, a.payoff);
-        acc[i].add(p);
-        acc2[i].add(p * p);
+        pay[i] = payoff_f32(s0 * expf(lg), f.strike, a.payoff);
       }
     }
-  }
-  store_partials<N>(a, acc, acc2);
+    return r.ok;
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -565,10 +665,8 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
   const float rho = f.h_rho, rho_comp = f.h_rho_comp, kappa_dt = f.h_kdt, theta = f.h_theta;
   const float xi_sdt = f.h_xsdt, sdt = f.h_sdt, mu_dt = f.h_mudt, nhdt = f.h_nhdt;
   unsigned err = 0;
-  Kahan acc[1], acc2[1];
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
   const uint32_t cap = uf_cap(2 * (uint32_t)a.steps);
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
+  run_rows<1>(a, [&](uint64_t base, float* pay) {
     WarpRow r = warp_row(a, base);
     ZigLane q;
     Plain lg;
@@ -593,13 +691,9 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
         }
       }
     });
-    if (r.ok) {
-      const float p = payoff_f32(f.h_s0 * expf(lg.value()), f.strike, a.payoff);
-      acc[0].add(p);
-      acc2[0].add(p * p);
-    }
-  }
-  store_partials<1>(a, acc, acc2);
+    if (r.ok) pay[0] = payoff_f32(f.h_s0 * expf(lg.value()), f.strike, a.payoff);
+    return r.ok;
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -614,10 +708,8 @@ __global__ void __launch_bounds__(256, kFusedMinBlocks) k_merton_uf(const __grid
   const float mu_j = f.m_mu_j, sigma_j = f.m_sigma_j;
   const uint64_t thr = a.merton.jump_thr;
   unsigned err = 0;
-  Kahan acc[1], acc2[1];
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
   const uint32_t cap = uf_cap(2 * (uint32_t)a.steps);
-  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < a.rows; base += nthreads) {
+  run_rows<1>(a, [&](uint64_t base, float* pay) {
     WarpRow r = warp_row(a, base);
     ZigLane q;
     Plain w;
@@ -641,13 +733,9 @@ __global__ void __launch_bounds__(256, kFusedMinBlocks) k_merton_uf(const __grid
         }
       }
     });
-    if (r.ok) {
-      const float p = payoff_f32(f.m_s0 * expf(fmaf(f.m_diff, w.value(), f.m_kdrift) + jumps), f.strike, a.payoff);
-      acc[0].add(p);
-      acc2[0].add(p * p);
-    }
-  }
-  store_partials<1>(a, acc, acc2);
+    if (r.ok) pay[0] = payoff_f32(f.m_s0 * expf(fmaf(f.m_diff, w.value(), f.m_kdrift) + jumps), f.strike, a.payoff);
+    return r.ok;
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -741,10 +829,18 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
     const uint64_t cap = (uint64_t)sms * per_sm * t.waves;
     if (g > cap) g = cap;
     if (g < 1) g = 1;
-    void* args[] = {(void*)&L};
+    // the loop and warp-uniform forms take their rows from the work queue
+    // when the caller supplies one; the lockstep form keeps its static rows
+    PathLaunch Lq = L;
+    const bool queue = L.work != nullptr && variant != 1 && L.batch_rows >= 32 && L.batch_rows % 32 == 0;
+    if (!queue) Lq.work = nullptr;
+    if (queue && cudaMemsetAsync(L.work, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
+    void* args[] = {(void*)&Lq};
     if (cudaLaunchKernel(fn, dim3((unsigned)g), dim3(t.block), args, 0, st) != cudaSuccess) return -1;
-    return (int)g;
+    return queue ? (int)((L.rows + L.batch_rows - 1) / L.batch_rows) : (int)g;
   }
+  PathLaunch Ls = L;  // the untuned kernels below run static rows
+  Ls.work = nullptr;
   const int b = 256;
   // Persistent grid: exactly the blocks that are resident at once, so the
   // grid-stride loop gives every thread the same number of paths (+-1) in a
@@ -765,17 +861,17 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
   dim3 G((unsigned)g), B(b);
   switch (L.model) {
     case kGbm:
-      if (store) k_gbm_f32<true><<<G, B, 0, st>>>(L); else k_gbm_f32<false><<<G, B, 0, st>>>(L);
+      if (store) k_gbm_f32<true><<<G, B, 0, st>>>(Ls); else k_gbm_f32<false><<<G, B, 0, st>>>(Ls);
       break;
     case kHeston:
       if (L.heston.scheme != 0) return -1;  // QE has no FP32 form
-      if (store) k_heston_euler_f32<true><<<G, B, 0, st>>>(L); else k_heston_euler_f32<false><<<G, B, 0, st>>>(L);
+      if (store) k_heston_euler_f32<true><<<G, B, 0, st>>>(Ls); else k_heston_euler_f32<false><<<G, B, 0, st>>>(Ls);
       break;
     case kMerton:
-      if (store) k_merton_f32<true><<<G, B, 0, st>>>(L); else k_merton_f32<false><<<G, B, 0, st>>>(L);
+      if (store) k_merton_f32<true><<<G, B, 0, st>>>(Ls); else k_merton_f32<false><<<G, B, 0, st>>>(Ls);
       break;
     case kMultiGbm:
-      if (store) launch_multi32<true>(L, G, B, st); else launch_multi32<false>(L, G, B, st);
+      if (store) launch_multi32<true>(Ls, G, B, st); else launch_multi32<false>(Ls, G, B, st);
       break;
     default:
       return -1;

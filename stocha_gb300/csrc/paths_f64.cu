@@ -277,14 +277,22 @@ __global__ void k_debug_exp(const double* __restrict__ x, double* __restrict__ y
     y[i] = mul_exp(1.0, x[i], zs);
 }
 
-__global__ void k_reduce_partials(const double* __restrict__ partials, int nblocks, int nvals,
-                                  double* __restrict__ out) {
-  // one block; thread t owns value t; fixed summation order -> deterministic
-  for (int v = threadIdx.x; v < nvals; v += blockDim.x) {
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partials[(uint64_t)b * nvals + v];
-    out[v] = s;
+// Block v sums value v of all records: thread t adds records t, t + 256, ...
+// in order, then a shared-memory tree adds the 256 partial sums.  The order
+// depends only on the record count, so the result is deterministic.
+__global__ void __launch_bounds__(256) k_reduce_partials(const double* __restrict__ partials, int nblocks,
+                                                         int nvals, double* __restrict__ out) {
+  __shared__ double sh[256];
+  const int v = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += 256) s += partials[(uint64_t)b * nvals + v];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) out[v] = sh[0];
 }
 
 template <bool kStore>
@@ -349,7 +357,7 @@ void launch_debug_exp(const double* x, double* y, uint64_t n, const ZigTables* t
 }
 
 void launch_reduce_partials(const double* partials, int nblocks, int nvals, double* out, cudaStream_t st) {
-  k_reduce_partials<<<1, 64, 0, st>>>(partials, nblocks, nvals, out);
+  if (nvals > 0) k_reduce_partials<<<nvals, 256, 0, st>>>(partials, nblocks, nvals, out);
 }
 
 }  // namespace stocha
