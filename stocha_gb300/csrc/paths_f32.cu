@@ -391,20 +391,55 @@ __device__ __forceinline__ void group_rows(const PathLaunch& a, uint64_t l0, uin
   }
 }
 
+// Rows of a lockstep kernel: static groups of ILP rows l0 + j * nthreads
+// (store_partials per block), or, with ILP 1 and a work queue, the queue's
+// batches (run_rows).  group(l0, stride, ok, p) prices rows l0 + j * stride
+// into p[j * NV + i] and flags the rows that exist.
+template <int ILP, int NV, class Group>
+__device__ __forceinline__ void lockstep_rows(const PathLaunch& a, Group&& group) {
+  if constexpr (ILP == 1) {
+    if (a.work) {
+      run_rows<NV>(a, [&](uint64_t b, float* p) {
+        const uint64_t lrow = b + (threadIdx.x & 31u);
+        if (lrow >= a.rows) return false;
+        bool ok[1];
+        group(lrow, 0, ok, p);
+        return ok[0];
+      });
+      return;
+    }
+  }
+  Kahan acc[NV], acc2[NV];
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
+    bool ok[ILP];
+    float p[ILP * NV];
+    group(l0, nthreads, ok, p);
+#pragma unroll
+    for (int j = 0; j < ILP; ++j)
+      if (ok[j]) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+          acc[i].add(p[j * NV + i]);
+          acc2[i].add(p[j * NV + i] * p[j * NV + i]);
+        }
+      }
+  }
+  store_partials<NV>(a, acc, acc2);
+}
+
 template <int ILP>
 __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_gbm_fused(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   unsigned err = 0;
-  Kahan acc[1], acc2[1];
   const float s0 = a.f32.g_s0, diffusion = a.f32.g_diff, kdrift = a.f32.g_kdrift, strike = a.f32.strike;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
-    bool ok[ILP], neg[ILP];
+  lockstep_rows<ILP, 1>(a, [&](uint64_t l0, uint64_t stride, bool* ok, float* p) {
+    bool neg[ILP];
     PcgGen s[ILP];
     Plain w[ILP];
-    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+    group_rows<ILP>(a, l0, stride, ok, neg, s);
 #pragma unroll 1
     for (uint64_t k = 0; k < a.steps; ++k) {
       float z[ILP];
@@ -414,13 +449,8 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_gbm_fus
     }
 #pragma unroll
     for (int j = 0; j < ILP; ++j)
-      if (ok[j]) {
-        const float p = payoff_f32(s0 * expf(fmaf(diffusion, w[j].value(), kdrift)), strike, a.payoff);
-        acc[0].add(p);
-        acc2[0].add(p * p);
-      }
-  }
-  store_partials<1>(a, acc, acc2);
+      if (ok[j]) p[j] = payoff_f32(s0 * expf(fmaf(diffusion, w[j].value(), kdrift)), strike, a.payoff);
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -433,14 +463,12 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_heston_
   const float rho = f.h_rho, rho_comp = f.h_rho_comp, kappa_dt = f.h_kdt, theta = f.h_theta;
   const float xi_sdt = f.h_xsdt, sdt = f.h_sdt, mu_dt = f.h_mudt, nhdt = f.h_nhdt, s0 = f.h_s0;
   unsigned err = 0;
-  Kahan acc[1], acc2[1];
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
-    bool ok[ILP], neg[ILP];
+  lockstep_rows<ILP, 1>(a, [&](uint64_t l0, uint64_t stride, bool* ok, float* p) {
+    bool neg[ILP];
     PcgGen s[ILP];
     Plain lg[ILP];
     float v[ILP];
-    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+    group_rows<ILP>(a, l0, stride, ok, neg, s);
 #pragma unroll
     for (int j = 0; j < ILP; ++j) v[j] = f.h_v0;
 #pragma unroll 1
@@ -459,13 +487,8 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_heston_
     }
 #pragma unroll
     for (int j = 0; j < ILP; ++j)
-      if (ok[j]) {
-        const float p = payoff_f32(s0 * expf(lg[j].value()), f.strike, a.payoff);
-        acc[0].add(p);
-        acc2[0].add(p * p);
-      }
-  }
-  store_partials<1>(a, acc, acc2);
+      if (ok[j]) p[j] = payoff_f32(s0 * expf(lg[j].value()), f.strike, a.payoff);
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -478,14 +501,12 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_merton_
   const float diffusion = f.m_diff, kdrift = f.m_kdrift, mu_j = f.m_mu_j, sigma_j = f.m_sigma_j, s0 = f.m_s0;
   const uint64_t thr = a.merton.jump_thr;
   unsigned err = 0;
-  Kahan acc[1], acc2[1];
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
-    bool ok[ILP], neg[ILP];
+  lockstep_rows<ILP, 1>(a, [&](uint64_t l0, uint64_t stride, bool* ok, float* p) {
+    bool neg[ILP];
     PcgGen s[ILP];
     Plain w[ILP];
     float jumps[ILP];
-    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+    group_rows<ILP>(a, l0, stride, ok, neg, s);
 #pragma unroll
     for (int j = 0; j < ILP; ++j) jumps[j] = 0.0f;
 #pragma unroll 1
@@ -500,13 +521,8 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_merton_
     }
 #pragma unroll
     for (int j = 0; j < ILP; ++j)
-      if (ok[j]) {
-        const float p = payoff_f32(s0 * expf(fmaf(diffusion, w[j].value(), kdrift) + jumps[j]), f.strike, a.payoff);
-        acc[0].add(p);
-        acc2[0].add(p * p);
-      }
-  }
-  store_partials<1>(a, acc, acc2);
+      if (ok[j]) p[j] = payoff_f32(s0 * expf(fmaf(diffusion, w[j].value(), kdrift) + jumps[j]), f.strike, a.payoff);
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -517,13 +533,11 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_multi_f
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const F32K& f = a.f32;
   unsigned err = 0;
-  Kahan acc[NA], acc2[NA];
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t l0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; l0 < a.rows; l0 += nthreads * ILP) {
-    bool ok[ILP], neg[ILP];
+  lockstep_rows<ILP, NA>(a, [&](uint64_t l0, uint64_t stride, bool* ok, float* p) {
+    bool neg[ILP];
     PcgGen s[ILP];
     Plain w[ILP][NA];
-    group_rows<ILP>(a, l0, nthreads, ok, neg, s);
+    group_rows<ILP>(a, l0, stride, ok, neg, s);
 #pragma unroll 1
     for (uint64_t k = 0; k < a.steps; ++k) {
 #pragma unroll
@@ -542,13 +556,10 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_multi_f
           float eps = 0.0f;
 #pragma unroll
           for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[j][m].value(), eps);
-          const float p = payoff_f32(f.a_s0[i] * expf(fmaf(f.a_diff[i], eps, f.a_kdrift[i])), f.strike, a.payoff);
-          acc[i].add(p);
-          acc2[i].add(p * p);
+          p[j * NA + i] = payoff_f32(f.a_s0[i] * expf(fmaf(f.a_diff[i], eps, f.a_kdrift[i])), f.strike, a.payoff);
         }
       }
-  }
-  store_partials<NA>(a, acc, acc2);
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -829,10 +840,11 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
     const uint64_t cap = (uint64_t)sms * per_sm * t.waves;
     if (g > cap) g = cap;
     if (g < 1) g = 1;
-    // the loop and warp-uniform forms take their rows from the work queue
-    // when the caller supplies one; the lockstep form keeps its static rows
+    // every form but the two-path lockstep one takes its rows from the work
+    // queue when the caller supplies one
     PathLaunch Lq = L;
-    const bool queue = L.work != nullptr && variant != 1 && L.batch_rows >= 32 && L.batch_rows % 32 == 0;
+    const bool queue = L.work != nullptr && !(variant == 1 && t.ilp == 2) && L.batch_rows >= 32 &&
+                       L.batch_rows % 32 == 0;
     if (!queue) Lq.work = nullptr;
     if (queue && cudaMemsetAsync(L.work, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
     void* args[] = {(void*)&Lq};

@@ -152,10 +152,10 @@ def test_every_tuned_launch_shape(stocha, model):
 
 @pytest.mark.parametrize("model", ["gbm", "heston", "merton", "multi_gbm"])
 def test_work_queue_price_is_shape_independent(stocha, model):
-    """The loop and warp-uniform forms take batches of 32 rows from a work
-    queue and write one record per batch in a fixed lane order, so a form's
-    FP32 price is bit-identical run to run and across its block sizes and
-    grid waves, including row counts that leave a partial batch."""
+    """The single-path forms take batches of 32 rows from a work queue and
+    write one record per batch in a fixed lane order, so a form's FP32 price
+    is bit-identical run to run and across its block sizes and grid waves,
+    including row counts that leave a partial batch."""
     if model == "multi_gbm":
         p = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.15],
                  corr=[[1, .6, .3], [.6, 1, .5], [.3, .5, 1]], t=1.0)
@@ -166,7 +166,7 @@ def test_work_queue_price_is_shape_independent(stocha, model):
     try:
         for n in (1, 33, 200_017):
             kw = dict(strike=100.0, payoff="call", steps=30, n_paths=n, seed=11, precision="fp32")
-            for variant in (0, 2):
+            for variant in (0, 1, 2):
                 got = set()
                 for block in (64, 256):
                     for waves in (1, 2):
