@@ -177,3 +177,22 @@ def test_work_queue_price_is_shape_independent(stocha, model):
     finally:
         stocha.tune_set(model, before["block"], before["ilp"], before["waves"], variant=before["variant"],
                         n_assets=na)
+
+
+@pytest.mark.parametrize("model", ["gbm", "multi_gbm"])
+def test_work_queue_multi_row_batches(stocha, model):
+    """Above 32 * 65536 rows a queue batch holds several 32-row groups per
+    warp (here 64 rows, the last batch partial): every row is priced once."""
+    if model == "multi_gbm":
+        p = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.15],
+                 corr=[[1, .6, .3], [.6, 1, .5], [.3, .5, 1]], t=1.0)
+    else:
+        p = MODELS[model]
+    kw = dict(strike=100.0, payoff="call", steps=4, n_paths=2_100_001, seed=5)
+    got = stocha.price_european(model, p, precision="fp32", **kw)
+    again = stocha.price_european(model, p, precision="fp32", **kw)
+    want = stocha.price_european(model, p, precision="fp64", **kw)
+    pairs = zip(got, want) if model == "multi_gbm" else [(got, want)]
+    for (g, _), (w, _) in pairs:
+        assert abs(g - w) <= 1e-5 * abs(w), (g, w)
+    assert repr(got) == repr(again)
