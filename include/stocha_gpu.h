@@ -145,7 +145,10 @@ int stocha_paths_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, i
  * (the same reduction greeks.rs:313-320 mc_price performs). */
 int stocha_price(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
                  double strike, double rate, double* out);
-/* Asynchronous form: out_dev is a device buffer of 2*n_assets doubles. */
+/* Asynchronous form: out_dev is a device buffer of 2*n_assets doubles.
+ * FP32: the result is the same bits run to run and for every launch shape
+ * of a kernel form (rows are priced in 32-row batches from a work queue and
+ * each batch's sums are added in a fixed order). */
 int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, int32_t precision, int32_t payoff,
                         double strike, double rate, double* out_dev);
 
