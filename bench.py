@@ -384,7 +384,15 @@ def bench_extras(stocha, torch, cores, skip_cpu):
                  ("asian_arith_fixed_call_cv", lambda n: stocha.asian_price(100, 100, .05, .2, 1., method="mc", n_paths=n),
                   None),
                  ("lookback_floating_call", lambda n: stocha.lookback_price(100, .05, .2, 1., method="mc", n_paths=n),
-                  lambda n: O.lookback_mc(100, .05, .2, 1., n_paths=n, threads=cores))]
+                  lambda n: O.lookback_mc(100, .05, .2, 1., n_paths=n, threads=cores)),
+                 # the FP32 forms (a GB300 addition: same draws, log-space FP32 paths)
+                 ("barrier_uo_call_h120_fp32", lambda n: stocha.barrier_price(100, 100, .05, .2, 1., 120, method="mc",
+                                                                              n_paths=n, n_steps=252,
+                                                                              precision="fp32"), None),
+                 ("asian_arith_fixed_call_cv_fp32", lambda n: stocha.asian_price(100, 100, .05, .2, 1., method="mc",
+                                                                                n_paths=n, precision="fp32"), None),
+                 ("lookback_floating_call_fp32", lambda n: stocha.lookback_price(100, .05, .2, 1., method="mc",
+                                                                                n_paths=n, precision="fp32"), None)]
         for name, gpu, cpu in cases:
             gpu(10_000)
             t0 = time.perf_counter()

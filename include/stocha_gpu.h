@@ -269,19 +269,23 @@ int stocha_rng_raw_u64(stocha_ctx* ctx, stocha_rng* rng, uint64_t size, uint64_t
  * the host (they are a few hundred flops); "mc" (and "auto" where the
  * reference falls back to it) runs the FP64 Monte Carlo kernel on the
  * device with the reference's streams.  Optional arguments: n_monitoring < 0
- * is None; running_avg, time_elapsed, running_max, running_min NaN is None. */
+ * is None; running_avg, time_elapsed, running_max, running_min NaN is None.
+ * precision: STOCHA_FP64 (the reference's arithmetic) or STOCHA_FP32 (a GB300
+ * addition: the same draws, paths carried in log space in FP32; barrier
+ * decisions can differ from FP64 only for paths within ~1e-7 of the barrier
+ * in log price).  The closed forms ignore it. */
 int stocha_barrier_price(stocha_ctx* ctx, double s, double k, double r, double sigma, double t, double barrier,
                          const char* barrier_type, const char* option_type, double q, uint64_t n_paths,
                          uint64_t n_steps, uint64_t seed, const char* method, int32_t n_monitoring, double rebate,
-                         int32_t rebate_at_hit, double* price);
+                         int32_t rebate_at_hit, int32_t precision, double* price);
 int stocha_asian_price(stocha_ctx* ctx, double s, double k, double r, double sigma, double t, uint64_t n_steps,
                        const char* average_type, const char* strike_type, const char* option_type, double q,
                        uint64_t n_paths, uint64_t seed, const char* method, double running_avg, double time_elapsed,
-                       double* price);
+                       int32_t precision, double* price);
 int stocha_lookback_price(stocha_ctx* ctx, double s, double r, double sigma, double t, uint64_t n_steps,
                           const char* strike_type, const char* option_type, double k, double q, uint64_t n_paths,
                           uint64_t seed, const char* method, double running_max, double running_min,
-                          double* price);
+                          int32_t precision, double* price);
 
 /* --------------------------------------------------------------- VaR/CVaR
  * replaces var_cvar (src/lib.rs:505-520, src/risk/var_cvar.rs:7-43):

@@ -156,34 +156,39 @@ def greeks_pathwise(s0: float, r: float, sigma: float, t: float, strike: float, 
 def barrier_price(s: float, k: float, r: float, sigma: float, t: float, barrier: float,
                   barrier_type: str = "up-and-out", option_type: str = "call", q: float = 0.0, n_paths: int = 100_000,
                   n_steps: int = 252, seed: int = 42, method: str = "auto", n_monitoring: int | None = None,
-                  rebate: float = 0.0, rebate_at_hit: bool = False) -> float:
+                  rebate: float = 0.0, rebate_at_hit: bool = False, precision: str = "fp64") -> float:
     """Barrier option price (python/stocha/__init__.py:983-1060): Reiner-Rubinstein closed form
-    ("auto"/"analytical") or Monte Carlo on the GPU ("mc")."""
+    ("auto"/"analytical") or Monte Carlo on the GPU ("mc").  ``precision="fp32"`` is a GB300
+    addition: the Monte Carlo paths in FP32 log space on the same draws."""
     return _stocha.barrier_price(s, k, r, sigma, t, barrier, barrier_type=barrier_type, option_type=option_type,
                                  q=q, n_paths=n_paths, n_steps=n_steps, seed=seed, method=method,
-                                 n_monitoring=n_monitoring, rebate=rebate, rebate_at_hit=rebate_at_hit)
+                                 n_monitoring=n_monitoring, rebate=rebate, rebate_at_hit=rebate_at_hit,
+                                 precision=precision)
 
 
 def asian_price(s: float, k: float, r: float, sigma: float, t: float, n_steps: int = 252,
                 average_type: str = "arithmetic", strike_type: str = "fixed", option_type: str = "call", q: float = 0.0,
                 n_paths: int = 100_000, seed: int = 42, method: str = "auto", running_avg: float | None = None,
-                time_elapsed: float | None = None) -> float:
+                time_elapsed: float | None = None, precision: str = "fp64") -> float:
     """Asian option price (python/stocha/__init__.py:1063-1127): Kemna-Vorst closed form for the
-    geometric fixed-strike case, Monte Carlo on the GPU (geometric control variate) otherwise."""
+    geometric fixed-strike case, Monte Carlo on the GPU (geometric control variate) otherwise.
+    ``precision="fp32"``: the Monte Carlo paths in FP32 (a GB300 addition)."""
     return _stocha.asian_price(s, k, r, sigma, t, n_steps=n_steps, average_type=average_type,
                                strike_type=strike_type, option_type=option_type, q=q, n_paths=n_paths, seed=seed,
-                               method=method, running_avg=running_avg, time_elapsed=time_elapsed)
+                               method=method, running_avg=running_avg, time_elapsed=time_elapsed,
+                               precision=precision)
 
 
 def lookback_price(s: float, r: float, sigma: float, t: float, n_steps: int = 252, strike_type: str = "floating",
                    option_type: str = "call", k: float = 0.0, q: float = 0.0, n_paths: int = 100_000, seed: int = 42,
                    method: str = "auto", running_max: float | None = None,
-                   running_min: float | None = None) -> float:
+                   running_min: float | None = None, precision: str = "fp64") -> float:
     """Lookback option price (python/stocha/__init__.py:1130-1190): Goldman-Sosin-Gatto / Conze-Viswanathan
-    closed forms or Monte Carlo on the GPU."""
+    closed forms or Monte Carlo on the GPU.  ``precision="fp32"``: the Monte Carlo paths in FP32
+    (a GB300 addition)."""
     return _stocha.lookback_price(s, r, sigma, t, n_steps=n_steps, strike_type=strike_type, option_type=option_type,
                                   k=k, q=q, n_paths=n_paths, seed=seed, method=method, running_max=running_max,
-                                  running_min=running_min)
+                                  running_min=running_min, precision=precision)
 
 
 def gaussian_copula(corr: np.ndarray, n_samples: int, seed: int = 42) -> np.ndarray:

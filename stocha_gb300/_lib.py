@@ -127,11 +127,11 @@ SIGNATURES = [
     ("stocha_greeks_batch", c_i32, [c_void_p, ctypes.POINTER(StochaGreeksInstance), c_u64, c_i32, P_dbl]),
     ("stocha_price_noalloc", c_i32, [ctypes.POINTER(StochaModel), c_u64, c_i32, c_i32, c_dbl, c_void_p, c_void_p]),
     ("stocha_barrier_price", c_i32, [c_void_p] + [c_dbl] * 6 + [c_char_p, c_char_p, c_dbl, c_u64, c_u64, c_u64,
-                                                                 c_char_p, c_i32, c_dbl, c_i32, P_dbl]),
+                                                                 c_char_p, c_i32, c_dbl, c_i32, c_i32, P_dbl]),
     ("stocha_asian_price", c_i32, [c_void_p] + [c_dbl] * 5 + [c_u64, c_char_p, c_char_p, c_char_p, c_dbl, c_u64,
-                                                               c_u64, c_char_p, c_dbl, c_dbl, P_dbl]),
+                                                               c_u64, c_char_p, c_dbl, c_dbl, c_i32, P_dbl]),
     ("stocha_lookback_price", c_i32, [c_void_p] + [c_dbl] * 4 + [c_u64, c_char_p, c_char_p, c_dbl, c_dbl, c_u64,
-                                                                  c_u64, c_char_p, c_dbl, c_dbl, P_dbl]),
+                                                                  c_u64, c_char_p, c_dbl, c_dbl, c_i32, P_dbl]),
     ("stocha_var_cvar", c_i32, [c_void_p, P_dbl, c_u64, c_dbl, P_dbl]),
     ("stocha_var_cvar_device", c_i32, [c_void_p, c_void_p, c_u64, c_dbl, P_dbl]),
     ("stocha_autotune", c_i32, [c_void_p, ctypes.POINTER(StochaModel), c_i32, ctypes.POINTER(StochaTuneResult)]),

@@ -309,10 +309,19 @@ def _opt_f64(x, name):
     return float("nan") if x is None else _f64(x, name)
 
 
+def _exotic_precision(precision):
+    if precision not in ("fp64", "fp32"):
+        raise ValueError("precision must be 'fp64' or 'fp32'")
+    return _lib.FP32 if precision == "fp32" else _lib.FP64
+
+
 def barrier_price(s, k, r, sigma, t, barrier, barrier_type="up-and-out", option_type="call", q=0.0,
                   n_paths=100_000, n_steps=252, seed=42, method="auto", n_monitoring=None, rebate=0.0,
-                  rebate_at_hit=False):
-    """lib.rs:1549-1641: barrier option price (analytical or Monte Carlo)."""
+                  rebate_at_hit=False, precision="fp64"):
+    """lib.rs:1549-1641: barrier option price (analytical or Monte Carlo).
+    ``precision="fp32"`` (no counterpart in the reference) runs the Monte
+    Carlo paths in FP32 log space on the same draws."""
+    prec = _exotic_precision(precision)
     vals = [_f64(v, nm) for v, nm in zip((s, k, r, sigma, t, barrier), ("s", "k", "r", "sigma", "t", "barrier"))]
     barrier_type, option_type = _str(barrier_type, "barrier_type"), _str(option_type, "option_type")
     q = _f64(q, "q")
@@ -322,13 +331,17 @@ def barrier_price(s, k, r, sigma, t, barrier, barrier_type="up-and-out", option_
     rebate, rebate_at_hit = _f64(rebate, "rebate"), _bool(rebate_at_hit, "rebate_at_hit")
     out = ctypes.c_double(0.0)
     check(load().stocha_barrier_price(None, *vals, barrier_type.encode(), option_type.encode(), q, n_paths, n_steps,
-                                      seed, method.encode(), n_mon, rebate, int(rebate_at_hit), ctypes.byref(out)))
+                                      seed, method.encode(), n_mon, rebate, int(rebate_at_hit), prec,
+                                      ctypes.byref(out)))
     return float(out.value)
 
 
 def asian_price(s, k, r, sigma, t, n_steps=252, average_type="arithmetic", strike_type="fixed", option_type="call",
-                q=0.0, n_paths=100_000, seed=42, method="auto", running_avg=None, time_elapsed=None):
-    """lib.rs:1643-1757: Asian option price (Kemna-Vorst or Monte Carlo)."""
+                q=0.0, n_paths=100_000, seed=42, method="auto", running_avg=None, time_elapsed=None,
+                precision="fp64"):
+    """lib.rs:1643-1757: Asian option price (Kemna-Vorst or Monte Carlo).
+    ``precision="fp32"``: the Monte Carlo paths in FP32 (a GB300 addition)."""
+    prec = _exotic_precision(precision)
     vals = [_f64(v, nm) for v, nm in zip((s, k, r, sigma, t), ("s", "k", "r", "sigma", "t"))]
     n_steps = _usize(n_steps, "n_steps")
     average_type, strike_type = _str(average_type, "average_type"), _str(strike_type, "strike_type")
@@ -338,13 +351,15 @@ def asian_price(s, k, r, sigma, t, n_steps=252, average_type="arithmetic", strik
     check(load().stocha_asian_price(None, *vals, n_steps, average_type.encode(), strike_type.encode(),
                                     option_type.encode(), q, n_paths, seed, method.encode(),
                                     _opt_f64(running_avg, "running_avg"), _opt_f64(time_elapsed, "time_elapsed"),
-                                    ctypes.byref(out)))
+                                    prec, ctypes.byref(out)))
     return float(out.value)
 
 
 def lookback_price(s, r, sigma, t, n_steps=252, strike_type="floating", option_type="call", k=0.0, q=0.0,
-                   n_paths=100_000, seed=42, method="auto", running_max=None, running_min=None):
-    """lib.rs:1759-1870: lookback option price (GSG / Conze-Viswanathan or Monte Carlo)."""
+                   n_paths=100_000, seed=42, method="auto", running_max=None, running_min=None, precision="fp64"):
+    """lib.rs:1759-1870: lookback option price (GSG / Conze-Viswanathan or Monte Carlo).
+    ``precision="fp32"``: the Monte Carlo paths in FP32 (a GB300 addition)."""
+    prec = _exotic_precision(precision)
     vals = [_f64(v, nm) for v, nm in zip((s, r, sigma, t), ("s", "r", "sigma", "t"))]
     n_steps = _usize(n_steps, "n_steps")
     strike_type, option_type = _str(strike_type, "strike_type"), _str(option_type, "option_type")
@@ -353,7 +368,7 @@ def lookback_price(s, r, sigma, t, n_steps=252, strike_type="floating", option_t
     out = ctypes.c_double(0.0)
     check(load().stocha_lookback_price(None, *vals, n_steps, strike_type.encode(), option_type.encode(), k, q, n_paths,
                                        seed, method.encode(), _opt_f64(running_max, "running_max"),
-                                       _opt_f64(running_min, "running_min"), ctypes.byref(out)))
+                                       _opt_f64(running_min, "running_min"), prec, ctypes.byref(out)))
     return float(out.value)
 
 

@@ -113,6 +113,91 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
   if (err) atomicOr(a.err, err);
 }
 
+// FP32 form of k_exotic (a GB300 addition; the reference prices in FP64).
+// The same streams and draws (the FP32 sampler consumes exactly the
+// reference's u64s); the path is carried in log space, ls = ln(S_t / s0) as a
+// plain FP32 running sum of drift + diffusion * z, so the barrier test is
+// ls against ln(H / s0) and the running extremes are extremes of ls, with
+// one exp per path; the Asian average takes one FP32 exp per step.  Values
+// differ from the FP64 form by rounding: a barrier decision can flip only for
+// a path within ~1e-7 (in log price) of the barrier at a monitoring date.
+__global__ void __launch_bounds__(128) k_exotic_f32(const __grid_constant__ ExoticLaunch a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  double sum = 0.0;
+  const float drift = (float)a.drift, diffusion = (float)a.diffusion, s0 = (float)a.s0, k = (float)a.k;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    PcgGen g{pcg_path_state(a.ss, i), a.ss.inc_lo, a.ss.inc_hi};
+    float ls = 0.0f;
+    if (a.kind == kExoBarrier) {
+      const float lb = (float)a.lbarrier;
+      int hit = -1;
+      if (a.already_hit) {
+        hit = 0;
+      } else {
+        for (uint64_t st = 1; st <= a.steps; ++st) {
+          ls += fmaf(diffusion, normal_f32(g, c, zs, err), drift);
+          if (a.direction == 0 ? ls >= lb : ls <= lb) {
+            hit = (int)st;
+            break;
+          }
+        }
+      }
+      const bool knocked = hit >= 0;
+      if (knocked && a.kind_in && (uint64_t)hit < a.steps)
+        for (uint64_t st = (uint64_t)hit; st < a.steps; ++st) ls += fmaf(diffusion, normal_f32(g, c, zs, err), drift);
+      const float sT = s0 * expf(ls);
+      const float iv = a.is_call ? fmaxf(sT - k, 0.0f) : fmaxf(k - sT, 0.0f);
+      const float opt = a.kind_in ? (knocked ? iv : 0.0f) : (knocked ? 0.0f : iv);
+      const double rpv = a.rebate == 0.0 ? 0.0 : rebate_pv(a, hit);
+      sum += (double)opt + rpv / a.discount;
+    } else if (a.kind == kExoLookback) {
+      float lmx = (float)a.lm0, lmn = (float)a.ln0;
+      for (uint64_t st = 0; st < a.steps; ++st) {
+        ls += fmaf(diffusion, normal_f32(g, c, zs, err), drift);
+        lmx = fmaxf(lmx, ls);
+        lmn = fminf(lmn, ls);
+      }
+      const float s = s0 * expf(ls), mx = s0 * expf(lmx), mn = s0 * expf(lmn);
+      sum += a.strike_fixed ? (a.is_call ? fmaxf(mx - k, 0.0f) : fmaxf(k - mn, 0.0f))
+                            : (a.is_call ? s - mn : mx - s);
+    } else {  // Asian: plain (per-path pair) or floating seasoned (block sum)
+      float sum_arith = 0.0f, sum_log = 0.0f;
+      for (uint64_t st = 0; st < a.steps; ++st) {
+        ls += fmaf(diffusion, normal_f32(g, c, zs, err), drift);
+        sum_arith += expf(ls);
+        sum_log += ls;
+      }
+      const double nsteps = (double)a.steps;
+      const double s = (double)s0 * exp((double)ls);
+      const double avg_a = a.s0 * (double)sum_arith / nsteps;
+      const double avg_g = a.s0 * exp((double)sum_log / nsteps);
+      if (a.kind == kExoAsian) {
+        double pa, pg;
+        if (!a.strike_floating) {
+          pa = intrinsic(avg_a, a.k, a.is_call);
+          pg = intrinsic(avg_g, a.k, a.is_call);
+        } else {
+          pa = a.is_call ? fmax(s - avg_a, 0.0) : fmax(avg_a - s, 0.0);
+          pg = a.is_call ? fmax(s - avg_g, 0.0) : fmax(avg_g - s, 0.0);
+        }
+        a.arith[i] = pa;
+        a.geo[i] = pg;
+      } else {  // kExoAsianSeasoned (floating strike)
+        const double avg_rem = a.geometric ? avg_g : avg_a;
+        const double avg_t = a.geometric ? exp(log(a.a_spent) * a.w_spent + log(avg_rem) * a.w_remain)
+                                         : a.w_spent * a.a_spent + a.w_remain * avg_rem;
+        sum += a.is_call ? fmax(s - avg_t, 0.0) : fmax(avg_t - s, 0.0);
+      }
+    }
+  }
+  if (a.kind != kExoAsian) block_sum2_store(sum, 0.0, a.partials + 2 * (uint64_t)blockIdx.x);
+  if (err) atomicOr(a.err, err);
+}
+
 // Sums over the Asian payoff pairs: mode 0 {sum a, sum g}; mode 1, with the
 // means m = {ma, mg}: {sum (a - ma)(g - mg), sum (g - mg)^2} (asian.rs:270-281).
 __global__ void __launch_bounds__(256) k_asian_sums(const double* __restrict__ arith, const double* __restrict__ geo,
@@ -149,7 +234,12 @@ int exotic_grid(uint64_t n, int sms) {
   return (int)(want < cap ? (want ? want : 1) : cap);
 }
 
-void launch_exotic(const ExoticLaunch& a, int grid, cudaStream_t st) { k_exotic<<<grid, 128, 0, st>>>(a); }
+void launch_exotic(const ExoticLaunch& a, int grid, cudaStream_t st) {
+  if (a.f32)
+    k_exotic_f32<<<grid, 128, 0, st>>>(a);
+  else
+    k_exotic<<<grid, 128, 0, st>>>(a);
+}
 
 void launch_asian_sums(const double* arith, const double* geo, uint64_t n, int mode, const double* means,
                        double* partials, int grid, cudaStream_t st) {

@@ -56,6 +56,7 @@ struct Barrier {
   int n_mon;   // <= 0: continuous
   double rebate;
   int at_hit;
+  int f32 = 0;  // Monte Carlo in the FP32 form
 };
 
 double hit_probability(double s, double h, double r, double q, double sigma, double t, bool up) {  // barrier.rs:48-66
@@ -159,6 +160,7 @@ struct Asian {
   uint64_t n_steps;
   int geometric, floating, call;
   double running_avg, time_elapsed;  // NaN: none
+  int f32 = 0;  // Monte Carlo in the FP32 form
 };
 
 bool seasoning(const Asian& p, double* a, double* t1) {  // asian.rs:44-50
@@ -229,6 +231,7 @@ struct Lookback {
   uint64_t n_steps;
   int fixed, call;
   double running_max, running_min;  // NaN: none
+  int f32 = 0;  // Monte Carlo in the FP32 form
 };
 
 double lb_d1(double s, double x, double r, double q, double sigma, double t) {  // lookback.rs:40-43
@@ -345,6 +348,8 @@ int barrier_mc(stocha_ctx* c, const Barrier& p, uint64_t n, uint64_t steps, uint
   a.rebate = p.rebate;
   a.rebate_at_hit = p.at_hit;
   a.already_hit = p.up ? p.s >= p.h : p.s <= p.h;
+  a.f32 = p.f32;
+  a.lbarrier = std::log(p.h / p.s);
   double total = 0.0;
   int rc = n ? run_sum(c, a, &total) : STOCHA_OK;
   if (rc) return rc;
@@ -358,6 +363,9 @@ int lookback_mc(stocha_ctx* c, const Lookback& p, uint64_t n, uint64_t seed, dou
   a.is_call = p.call;
   a.m0 = std::fmax(std::isnan(p.running_max) ? p.s : p.running_max, p.s);  // lookback.rs:185-186
   a.n0 = std::fmin(std::isnan(p.running_min) ? p.s : p.running_min, p.s);
+  a.f32 = p.f32;
+  a.lm0 = std::log(a.m0 / p.s);
+  a.ln0 = std::log(a.n0 / p.s);
   double total = 0.0;
   int rc = n ? run_sum(c, a, &total) : STOCHA_OK;
   if (rc) return rc;
@@ -378,6 +386,7 @@ int asian_floating_seasoned(stocha_ctx* c, const Asian& p, double a_spent, doubl
   a.a_spent = a_spent;
   a.w_spent = t1 / p.t;
   a.w_remain = rem / p.t;
+  a.f32 = p.f32;
   double total = 0.0;
   int rc = n ? run_sum(c, a, &total) : STOCHA_OK;
   if (rc) return rc;
@@ -421,6 +430,7 @@ int asian_mc(stocha_ctx* c, const Asian& p, uint64_t n, uint64_t seed, double* o
   ExoticLaunch a = base_launch(c, p.s, p.k, p.r, p.q, p.sigma, p.t, p.n_steps, n, seed, kExoAsian);
   a.strike_floating = p.floating;
   a.is_call = p.call;
+  a.f32 = p.f32;
   const bool use_cv = !p.geometric && !p.floating;
   double geo_analytical = 0.0;
   if (use_cv) {
@@ -482,8 +492,10 @@ extern "C" {
 int stocha_barrier_price(stocha_ctx* ctx, double s, double k, double r, double sigma, double t, double barrier,
                          const char* barrier_type, const char* option_type, double q, uint64_t n_paths,
                          uint64_t n_steps, uint64_t seed, const char* method, int32_t n_monitoring, double rebate,
-                         int32_t rebate_at_hit, double* price) {
+                         int32_t rebate_at_hit, int32_t precision, double* price) {
   STOCHA_RANGE("stocha_barrier_price");
+  if (precision != STOCHA_FP64 && precision != STOCHA_FP32)
+    return set_error(STOCHA_ERR_VALUE, "precision must be 'fp64' or 'fp32'");
   // lib.rs:1567-1582
   if (s <= 0.0) return set_error(STOCHA_ERR_VALUE, "s must be positive");
   if (k <= 0.0) return set_error(STOCHA_ERR_VALUE, "k must be positive");
@@ -508,6 +520,7 @@ int stocha_barrier_price(stocha_ctx* ctx, double s, double k, double r, double s
   p.n_mon = n_monitoring;
   p.rebate = rebate;
   p.at_hit = rebate_at_hit ? 1 : 0;
+  p.f32 = precision == STOCHA_FP32;
   const std::string m = method ? method : "";
   int rc;
   if (m == "auto" || m == "analytical") {  // lib.rs:1618-1630
@@ -530,8 +543,10 @@ int stocha_barrier_price(stocha_ctx* ctx, double s, double k, double r, double s
 int stocha_asian_price(stocha_ctx* ctx, double s, double k, double r, double sigma, double t, uint64_t n_steps,
                        const char* average_type, const char* strike_type, const char* option_type, double q,
                        uint64_t n_paths, uint64_t seed, const char* method, double running_avg, double time_elapsed,
-                       double* price) {
+                       int32_t precision, double* price) {
   STOCHA_RANGE("stocha_asian_price");
+  if (precision != STOCHA_FP64 && precision != STOCHA_FP32)
+    return set_error(STOCHA_ERR_VALUE, "precision must be 'fp64' or 'fp32'");
   // lib.rs:1664-1716
   if (s <= 0.0) return set_error(STOCHA_ERR_VALUE, "s must be positive");
   if (k <= 0.0) return set_error(STOCHA_ERR_VALUE, "k must be positive");
@@ -556,6 +571,7 @@ int stocha_asian_price(stocha_ctx* ctx, double s, double k, double r, double sig
   p.s = s, p.k = k, p.r = r, p.q = q, p.sigma = sigma, p.t = t, p.n_steps = n_steps;
   p.running_avg = running_avg;
   p.time_elapsed = time_elapsed;
+  p.f32 = precision == STOCHA_FP32;
   const bool has_analytical = p.geometric && !p.floating;
   const std::string m = method ? method : "";
   int rc;
@@ -585,8 +601,10 @@ int stocha_asian_price(stocha_ctx* ctx, double s, double k, double r, double sig
 int stocha_lookback_price(stocha_ctx* ctx, double s, double r, double sigma, double t, uint64_t n_steps,
                           const char* strike_type, const char* option_type, double k, double q, uint64_t n_paths,
                           uint64_t seed, const char* method, double running_max, double running_min,
-                          double* price) {
+                          int32_t precision, double* price) {
   STOCHA_RANGE("stocha_lookback_price");
+  if (precision != STOCHA_FP64 && precision != STOCHA_FP32)
+    return set_error(STOCHA_ERR_VALUE, "precision must be 'fp64' or 'fp32'");
   // lib.rs:1779-1814
   if (s <= 0.0) return set_error(STOCHA_ERR_VALUE, "s must be positive");
   if (sigma <= 0.0) return set_error(STOCHA_ERR_VALUE, "sigma must be positive");
@@ -609,6 +627,7 @@ int stocha_lookback_price(stocha_ctx* ctx, double s, double r, double sigma, dou
   p.s = s, p.k = k, p.r = r, p.q = q, p.sigma = sigma, p.t = t, p.n_steps = n_steps;
   p.running_max = running_max;
   p.running_min = running_min;
+  p.f32 = precision == STOCHA_FP32;
   const std::string m = method ? method : "";
   int rc;
   if (m == "auto" || m == "analytical") {  // lib.rs:1836-1847

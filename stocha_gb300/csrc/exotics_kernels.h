@@ -27,13 +27,14 @@ struct ExoticLaunch {
   int strike_floating;   // Asian
   int strike_fixed;      // lookback
   int geometric;         // seasoned Asian
-  int pad;
+  int f32;               // 1: the FP32 form (log-space paths, FP32 sampler)
   uint64_t n, steps;
   double s0, k, drift, diffusion, discount, dt, r;
   double barrier, rebate;
   double log_s0;                  // Asian: ln(s0)
   double m0, n0;                  // lookback: initial running max / min
   double a_spent, w_spent, w_remain;  // seasoned Asian
+  double lbarrier, lm0, ln0;          // FP32 form: ln(barrier / s0), ln(m0 / s0), ln(n0 / s0)
 };
 
 int exotic_grid(uint64_t n, int sms);

@@ -118,3 +118,15 @@ def test_asian_geometric_closed_form_and_seasoning(stocha):
         stocha.asian_price(100, 100, 0.05, 0.2, 1.0, average_type="harmonic")
     with pytest.raises(ValueError, match="only available for geometric average with fixed strike"):
         stocha.asian_price(100, 100, 0.05, 0.2, 1.0, method="analytical")
+
+
+def test_exotic_precision_validation(stocha):
+    """precision is checked before any CUDA call; the closed forms ignore it."""
+    with pytest.raises(ValueError, match="precision must be 'fp64' or 'fp32'"):
+        stocha.barrier_price(100, 100, .05, .2, 1., 120, method="mc", precision="fp16")
+    with pytest.raises(ValueError, match="precision must be 'fp64' or 'fp32'"):
+        stocha.asian_price(100, 100, .05, .2, 1., method="mc", precision="bf16")
+    with pytest.raises(ValueError, match="precision must be 'fp64' or 'fp32'"):
+        stocha.lookback_price(100, .05, .2, 1., method="mc", precision="half")
+    a = stocha.barrier_price(100, 100, .05, .2, 1., 120, method="analytical")
+    assert stocha.barrier_price(100, 100, .05, .2, 1., 120, method="analytical", precision="fp32") == a

@@ -124,3 +124,44 @@ def test_lookback_mc_reference_expectations(stocha):
     # a running minimum above spot has no closed form: "auto" falls back to the Monte Carlo
     p = stocha.lookback_price(100, 0.05, 0.2, 1.0, running_min=110.0, n_paths=50_000)
     assert math.isfinite(p) and p > 0
+
+
+# FP32 form (a GB300 addition): the same draws, log-space FP32 paths.  Lookback
+# and Asian prices are continuous in the path values, so they stay within
+# rounding of the FP64 form; a barrier decision flips only for a path within
+# ~1e-7 of the barrier in log price at a monitoring date, which moves the
+# price by a small fraction of its Monte Carlo standard error.
+FP32_RTOL = 2e-5
+FP32_BARRIER_RTOL = 3e-3
+
+
+@pytest.mark.parametrize("btype,h", [("up-and-out", 120.0), ("down-and-in", 90.0)])
+def test_barrier_fp32_close_to_fp64(stocha, btype, h):
+    kw = dict(s=100, k=100, r=.05, sigma=.2, t=1., barrier=h, barrier_type=btype, method="mc", n_paths=400_000,
+              n_steps=252, rebate=2.0)
+    p64 = stocha.barrier_price(**kw)
+    p32 = stocha.barrier_price(**kw, precision="fp32")
+    assert abs(p32 - p64) <= FP32_BARRIER_RTOL * abs(p64), (p32, p64)
+
+
+@pytest.mark.parametrize("avg,strike", [("arithmetic", "fixed"), ("geometric", "floating"),
+                                        ("arithmetic", "floating")])
+def test_asian_fp32_close_to_fp64(stocha, avg, strike):
+    kw = dict(s=100, k=100, r=.05, sigma=.2, t=1., n_steps=252, average_type=avg, strike_type=strike,
+              method="mc", n_paths=200_000)
+    p64 = stocha.asian_price(**kw)
+    p32 = stocha.asian_price(**kw, precision="fp32")
+    assert abs(p32 - p64) <= FP32_RTOL * abs(p64), (p32, p64)
+    # seasoned floating strike (the block-sum kind)
+    kw.update(strike_type="floating", running_avg=103.0, time_elapsed=0.3)
+    assert abs(stocha.asian_price(**kw, precision="fp32") - stocha.asian_price(**kw)) <= \
+        FP32_RTOL * abs(stocha.asian_price(**kw))
+
+
+@pytest.mark.parametrize("strike,opt", [("floating", "call"), ("fixed", "put")])
+def test_lookback_fp32_close_to_fp64(stocha, strike, opt):
+    kw = dict(s=100.0, r=0.05, sigma=0.3, t=0.75, n_steps=120, strike_type=strike, option_type=opt, k=100.0,
+              q=0.02, n_paths=200_000, seed=8, running_max=112.0, running_min=91.0, method="mc")
+    p64 = stocha.lookback_price(**kw)
+    p32 = stocha.lookback_price(**kw, precision="fp32")
+    assert abs(p32 - p64) <= FP32_RTOL * abs(p64), (p32, p64)
