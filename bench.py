@@ -693,7 +693,11 @@ def run_ours(args, rank, world):
                     "d2h_bytes_per_step": 8 * (6 + 2 + 2)},
             "gpu_launches": 6 * args.steps,
             "roofline": {"bound": "int (PCG64DXSM generator)", "achieved": achieved / 1e9, "peak": peak_draws.value / 1e9,
-                         "unit": "Gdraws/s", "frac": achieved / peak_draws.value, "traffic": None,
+                         "unit": "Gdraws/s", "frac": achieved / peak_draws.value,
+                         # dram__bytes_read.sum + dram__bytes_write.sum of one k_gbm_uf<3> launch
+                         # (ncu, profiles/k_gbm_uf3_fused_200k.md): the staged ziggurat tables only,
+                         # the same at any path count (no path data leaves the registers)
+                         "traffic": 77824, "traffic_unit": "bytes per launch (multi-GBM kernel)",
                          "kernel_ms": per_model, "peak_source": "measured live (stocha_measure_peak kind 3)"},
             "fp64_plain": fp64,
             "autotune": tuning,
