@@ -67,8 +67,8 @@ void build_tables(ZigTables* t) {
   }
   t->r = STOCHA_ZIG_R_HEX;
   t->r32 = (float)t->r;
-  static const double E2[256] = STOCHA_EXP2_TAB_INIT;
-  for (int j = 0; j < 256; ++j) t->exp2tab[j] = E2[j];
+  static const uint64_t E2[256] = STOCHA_EXP2_Q63_INIT;
+  for (int j = 0; j < 256; ++j) t->exp2q[j] = E2[j];
 }
 
 // Brown's arbitrary-stride LCG jump (rand_pcg advance, pcg64.rs:41-43):

@@ -38,7 +38,7 @@ struct ZigTables {
   double r;
   float r32;
   float pad_;
-  double exp2tab[256];  // 2^(j/256) of the table-driven exponential
+  uint64_t exp2q[256];  // 2^(j/256) * 2^63 (integer-pipe exponential)
 };
 
 // Device error bits (ORed into a per-context word).

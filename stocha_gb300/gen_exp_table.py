@@ -1,14 +1,15 @@
 #!/usr/bin/env python3
-"""Constants of the table-driven FP64 exponential of the path kernels.
+"""Constants of the FP64 kernels' exponential, evaluated on the integer pipes.
 
-Tang, "Table-driven implementation of the exponential function in IEEE
-floating-point arithmetic", ACM TOMS 15(2), 1989:
-    exp(t) = 2^(k/N) * exp(r),  k = round(t * N / ln 2),  r = t - k ln2/N,
-with N = 256, |r| <= ln2/512.  This script writes
-  * 2^(j/256), j = 0..255, each rounded once to the nearest double;
-  * N/ln2 (rounded);
-  * ln2/N split for an exact Cody-Waite reduction: HI keeps 35 significant
-    bits (k * HI is exact for |k| < 2^18, i.e. |t| < 700), LO = ln2/N - HI.
+Tang's table-driven reduction (ACM TOMS 15(2), 1989) in fixed point:
+    exp(t) = 2^(k/256) * exp(r),   k = floor(t * 256/ln2),   r = t - k ln2/256,
+so 0 <= r < ln2/256, and exp(r) - 1 by its degree-6 Taylor polynomial with
+non-negative terms (unsigned arithmetic throughout).  This script writes, each
+rounded once to the nearest integer:
+  * 2^(j/256) * 2^63, j = 0..255               (Q63 table)
+  * 256/ln2 * 2^54                             (Q54)
+  * ln2/256 * 2^72                             (Q72)
+  * 2^32/120, 2^32/720, 2^36/24, 2^64/6        (polynomial coefficients)
 
 Run:  python stocha_gb300/gen_exp_table.py > stocha_gb300/csrc/exp_table.inc
 (needs mpmath; the generated file is committed).
@@ -20,27 +21,27 @@ def main(out=sys.stdout):
     import mpmath as mp
 
     mp.mp.dps = 60
-    n = 256
     w = out.write
-    w("/* 2^(j/256) and reduction constants of the table-driven FP64 exponential.\n")
-    w("   Generated by stocha_gb300/gen_exp_table.py (mpmath, 60 digits); do not edit. */\n")
-    w("#define STOCHA_EXP2_TAB_INIT { \\\n")
-    for j in range(n):
-        v = float(mp.power(2, mp.mpf(j) / n))
-        w(f"  {v.hex()}{',' if j < n - 1 else ''} \\\n")
-    w("}\n")
-    inv = float(n / mp.log(2))
-    c = mp.log(2) / n
-    c_d = float(c)
-    # keep 35 significant bits: clear the low 18 of the 53
-    import struct
 
-    bits = struct.unpack("<Q", struct.pack("<d", c_d))[0] & ~((1 << 18) - 1)
-    hi = struct.unpack("<d", struct.pack("<Q", bits))[0]
-    lo = float(c - mp.mpf(hi))
-    w(f"#define STOCHA_EXP_INV_LN2_N {inv.hex()}\n")
-    w(f"#define STOCHA_EXP_LN2_N_HI {hi.hex()}\n")
-    w(f"#define STOCHA_EXP_LN2_N_LO {lo.hex()}\n")
+    def q(x, bits):
+        v = int(mp.nint(x * mp.mpf(2) ** bits))
+        assert 0 < v < 2**64
+        return v
+
+    w("/* Q63 table of 2^(j/256) and fixed-point constants of the integer-pipe\n")
+    w("   FP64 exponential.  Generated by stocha_gb300/gen_exp_table.py (mpmath,\n")
+    w("   60 digits); do not edit. */\n")
+    w("#define STOCHA_EXP2_Q63_INIT { \\\n")
+    for j in range(256):
+        w(f"  0x{q(mp.power(2, mp.mpf(j) / 256), 63):016x}ull{',' if j < 255 else ''} \\\n")
+    w("}\n")
+    ln2 = mp.log(2)
+    w(f"#define STOCHA_IEXP_C54 0x{q(256 / ln2, 54):016x}ull  /* 256/ln2, Q54 */\n")
+    w(f"#define STOCHA_IEXP_L72 0x{q(ln2 / 256, 72):016x}ull  /* ln2/256, Q72 */\n")
+    w(f"#define STOCHA_IEXP_C120 0x{q(mp.mpf(1) / 120, 32):08x}u  /* 1/120, Q32 */\n")
+    w(f"#define STOCHA_IEXP_C720 0x{q(mp.mpf(1) / 720, 32):08x}u  /* 1/720, Q32 */\n")
+    w(f"#define STOCHA_IEXP_C24 0x{q(mp.mpf(1) / 24, 36):08x}u  /* 1/24, Q36 */\n")
+    w(f"#define STOCHA_IEXP_C6 0x{q(mp.mpf(1) / 6, 64):016x}ull  /* 1/6, Q64 */\n")
 
 
 if __name__ == "__main__":

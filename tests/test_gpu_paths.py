@@ -163,9 +163,11 @@ def test_config2_prefix_rows_full_size(stocha, oracle):
 
 
 def test_table_exp_accuracy(stocha):
-    """The FP64 path kernels' exponential (table-driven, 2^(j/256) table plus
-    a degree-4 polynomial) against numpy's exp: <= 3 ulp over the working
-    range, exact special values, subnormal and overflow results."""
+    """The FP64 kernels' exponential (integer pipes: Tang's reduction in fixed
+    point, a Q63 2^(j/256) table, one rounding to 53 bits) against exp in
+    extended precision: <= 0.6 ulp of the true value for |t| < 16 (0.5 from the
+    final rounding, < 0.06 from the truncated fixed-point steps), <= 2 ulp beyond (exp() fallback, compared with numpy's), exact special
+    values, subnormal and overflow results."""
     import ctypes
 
     from stocha_gb300 import _lib
@@ -175,6 +177,11 @@ def test_table_exp_accuracy(stocha):
     x = np.concatenate([
         rng.uniform(-1, 1, 200_000), rng.uniform(-40, 40, 200_000), rng.uniform(-699.9, 699.9, 100_000),
         rng.normal(0, 1e-3, 50_000),
+        # reduction boundaries k ln2/256 and their neighbours (k = floor(t 256/ln2) flips there)
+        np.nextafter(np.arange(-2000, 2000) * np.log(2) / 256, -np.inf),
+        np.arange(-2000, 2000) * np.log(2) / 256,
+        np.nextafter(np.arange(-2000, 2000) * np.log(2) / 256, np.inf),
+        np.ldexp(1.0, np.arange(-70, 4)), -np.ldexp(1.0, np.arange(-70, 4)), [15.999999999999998, -15.999999999999998],
         np.array([0.0, -0.0, 1e-300, -1e-300, 0.5, 1.0, -1.0, 699.99, -699.99, 700.0, -700.0, 709.7, 710.0, -708.5,
                   -745.0, -800.0, np.inf, -np.inf, np.nan]),
     ])
@@ -184,8 +191,16 @@ def test_table_exp_accuracy(stocha):
     want = np.exp(x)
     fin = np.isfinite(want) & (want > np.finfo(float).tiny)
     ulp = np.abs(y[fin] - want[fin]) / np.spacing(want[fin])
-    assert ulp.max() <= 3.0, ulp.max()
-    assert y[x == 0.0].tolist() == [1.0, 1.0]
+    assert ulp.max() <= 2.0, ulp.max()
+    work = np.abs(x) < 16.0
+    assert work.sum() > 300_000
+    if np.finfo(np.longdouble).eps < 1e-18:  # x86 extended or quad precision
+        exact = np.exp(x[work].astype(np.longdouble))
+        err = np.abs(y[work].astype(np.longdouble) - exact) / np.spacing(exact.astype(np.float64)).astype(np.longdouble)
+        assert float(err.max()) <= 0.6, float(err.max())
+    else:
+        assert (np.abs(y[work] - want[work]) / np.spacing(want[work])).max() <= 1.05
+    assert (y[x == 0.0] == 1.0).all()
     assert np.isinf(y[x == np.inf]).all() and (y[x == -np.inf] == 0).all() and np.isnan(y[np.isnan(x)]).all()
     assert np.isinf(y[x == 710.0]).all()
     sub = (want > 0) & (want < np.finfo(float).tiny)
