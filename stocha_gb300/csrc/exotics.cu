@@ -33,6 +33,13 @@ __device__ __forceinline__ double rebate_pv(const ExoticLaunch& a, int hit) {
   return knocked ? 0.0 : a.rebate * exp(-a.r * ((double)a.steps * a.dt));
 }
 
+// a >= b for doubles known to be >= +0 (or b negative), by their bits on the
+// integer pipes: for non-negative IEEE doubles the order of the bit patterns
+// as signed integers is the numeric order, and any negative b compares below.
+__device__ __forceinline__ bool ge_pos(double a, double b) {
+  return __double_as_longlong(a) >= __double_as_longlong(b);
+}
+
 __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
@@ -50,8 +57,9 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       } else {
         for (uint64_t st = 1; st <= a.steps; ++st) {
           const double z = normal_f64(g, c, zs, err);
-          s = mul_exp(s, a.drift + a.diffusion * z, zs);
-          if (a.direction == 0 ? s >= a.barrier : s <= a.barrier) {
+          s = mul_exp(s, fma(a.diffusion, z, a.drift), zs);
+          // s > 0 and the barrier is validated positive
+          if (a.direction == 0 ? ge_pos(s, a.barrier) : ge_pos(a.barrier, s)) {
             hit = (int)st;
             break;
           }
@@ -61,7 +69,7 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       if (knocked && a.kind_in && (uint64_t)hit < a.steps)  // drive a knocked-in path to T
         for (uint64_t st = (uint64_t)hit; st < a.steps; ++st) {
           const double z = normal_f64(g, c, zs, err);
-          s = mul_exp(s, a.drift + a.diffusion * z, zs);
+          s = mul_exp(s, fma(a.diffusion, z, a.drift), zs);
         }
       const double opt = a.kind_in ? (knocked ? intrinsic(s, a.k, a.is_call) : 0.0)
                                    : (knocked ? 0.0 : intrinsic(s, a.k, a.is_call));
@@ -71,9 +79,10 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       double mx = a.m0, mn = a.n0;
       for (uint64_t st = 0; st < a.steps; ++st) {
         const double z = normal_f64(g, c, zs, err);
-        s = mul_exp(s, a.drift + a.diffusion * z, zs);
-        if (s > mx) mx = s;
-        if (s < mn) mn = s;
+        s = mul_exp(s, fma(a.diffusion, z, a.drift), zs);
+        // s > 0 and mx >= s0 > 0; mn may be any non-NaN value
+        if (!ge_pos(mx, s)) mx = s;
+        if (!ge_pos(s, mn)) mn = s;
       }
       sum += a.strike_fixed ? (a.is_call ? fmax(mx - a.k, 0.0) : fmax(a.k - mn, 0.0))
                             : (a.is_call ? s - mn : mx - s);
@@ -81,7 +90,7 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       double sum_arith = 0.0, sum_log = 0.0, lg = a.log_s0;
       for (uint64_t st = 0; st < a.steps; ++st) {
         const double z = normal_f64(g, c, zs, err);
-        const double x = a.drift + a.diffusion * z;
+        const double x = fma(a.diffusion, z, a.drift);
         s = mul_exp(s, x, zs);
         lg += x;
         sum_arith += s;

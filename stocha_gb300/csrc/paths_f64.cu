@@ -69,13 +69,14 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
-    const double drift = a.gbm.drift, diffusion = a.gbm.diffusion;
+    // the antithetic path's -z enters only through diffusion * z, so the sign
+    // goes on the coefficient once per path (exact: IEEE products are odd)
+    const double drift = a.gbm.drift, diffusion = neg ? -a.gbm.diffusion : a.gbm.diffusion;
     double x = a.gbm.s0;
     if (kStore) store64(a, lrow, 0, 1, 0, x);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
-      double z = normal_f64(s, c, zs, err);
-      if (neg) z = -z;
+      const double z = normal_f64(s, c, zs, err);
       x = mul_exp(x, fma(diffusion, z, drift), zs);
       if (kStore) store64(a, lrow, k, 1, 0, x);
     }
@@ -103,26 +104,25 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
-    double sv[NA > 0 ? NA : kMaxAssets], z[NA > 0 ? NA : kMaxAssets];
+    double sv[NA > 0 ? NA : kMaxAssets], z[NA > 0 ? NA : kMaxAssets], dif[NA > 0 ? NA : kMaxAssets];
 #pragma unroll
     for (int i = 0; i < na; ++i) {
       sv[i] = a.multi.s0[i];
+      // antithetic sign on the coefficient: L(-z) = -(L z) exactly
+      dif[i] = neg ? -a.multi.diffusion[i] : a.multi.diffusion[i];
       if (kStore) store64(a, lrow, 0, na, i, sv[i]);
     }
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
 #pragma unroll
       for (int i = 0; i < na; ++i) z[i] = normal_f64(s, c, zs, err);
-      if (neg) {
-#pragma unroll
-        for (int i = 0; i < na; ++i) z[i] = -z[i];
-      }
 #pragma unroll
       for (int i = 0; i < na; ++i) {
-        double eps = 0.0;
+        // row i of L z, one rounding per term
+        double eps = a.multi.L[i * kMaxAssets] * z[0];
 #pragma unroll
-        for (int m = 0; m <= i; ++m) eps += a.multi.L[i * kMaxAssets + m] * z[m];
-        sv[i] = mul_exp(sv[i], fma(a.multi.diffusion[i], eps, a.multi.drift[i]), zs);
+        for (int m = 1; m <= i; ++m) eps = fma(a.multi.L[i * kMaxAssets + m], z[m], eps);
+        sv[i] = mul_exp(sv[i], fma(dif[i], eps, a.multi.drift[i]), zs);
         if (kStore) store64(a, lrow, k, na, i, sv[i]);
       }
     }
@@ -156,6 +156,7 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
     double x = h.s0, v = h.v0;
     if (kStore) store64(a, lrow, 0, 1, 0, x);
     if (h.scheme == 0) {
+      const double mu_dt = h.mu * h.dt, nhalf_dt = -0.5 * h.dt;
 #pragma unroll 1
       for (uint64_t k = 1; k <= a.steps; ++k) {
         double dw1 = normal_f64(s, c, zs, err);
@@ -163,8 +164,11 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
         double dw2 = h.rho * dw1 + h.rho_comp * dz;
         double v_plus = fmax(v, 0.0);
         double sqrt_v = sqrt(v_plus);
+        // the variance recursion keeps the reference's operations and roundings
+        // (it feeds back through fmax(v, 0)); the log-price increment
+        // (mu - v+/2) dt + sqrt(v+ dt) dW1 only feeds x, so it is fused
         v += h.kappa * (h.theta - v_plus) * h.dt + h.xi * sqrt_v * h.sqrt_dt * dw2;
-        x = mul_exp(x, (h.mu - 0.5 * v_plus) * h.dt + sqrt_v * h.sqrt_dt * dw1, zs);
+        x = mul_exp(x, fma(sqrt_v * h.sqrt_dt, dw1, fma(nhalf_dt, v_plus, mu_dt)), zs);
         if (kStore) store64(a, lrow, k, 1, 0, x);
       }
     } else {
@@ -224,15 +228,14 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
     if (kStore) store64(a, lrow, 0, 1, 0, x);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
-      double z = normal_f64(s, c, zs, err);
-      double diffusion_return = M.drift + M.diffusion * z;
-      uint64_t u = s.next();
-      double jump_return = 0.0;
-      if ((u >> 11) < M.jump_thr) {
-        double z_j = normal_f64(s, c, zs, err);
-        jump_return = M.mu_j + M.sigma_j * z_j;
+      const double z = normal_f64(s, c, zs, err);
+      double ret = fma(M.diffusion, z, M.drift);
+      const uint64_t u = s.next();
+      if ((u >> 11) < M.jump_thr) {  // the reference adds a zero jump return otherwise
+        const double z_j = normal_f64(s, c, zs, err);
+        ret += fma(M.sigma_j, z_j, M.mu_j);
       }
-      x = mul_exp(x, diffusion_return + jump_return, zs);
+      x = mul_exp(x, ret, zs);
       if (kStore) store64(a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
