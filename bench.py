@@ -653,18 +653,28 @@ def run_ours(args, rank, world):
                 "bytes_written_per_step": 8 * N_PATHS * (STEPS + 1) * 5}
         if not args.skip_e2e64:
             corr = np.array(CORR3)
-            t0 = time.perf_counter()
-            x = stocha.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, N_PATHS, seed=seed)
-            del x
-            x = stocha.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")], STEPS,
-                              N_PATHS, seed=seed)
-            del x
-            x = stocha.merton_jump_diffusion(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j",
-                                                                   "sigma_j", "t")], STEPS, N_PATHS, seed=seed)
-            del x
-            e64 = max_over_ranks(time.perf_counter() - t0)
-            fp64["e2e"] = {"value": world * path_steps / e64, "unit": "path-steps/s",
-                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8 * N_PATHS * (STEPS + 1) * 5}
+
+            def e2e64_pass():
+                # each result is dropped before the next call, as a caller that
+                # reduces the paths and moves on would
+                t0 = time.perf_counter()
+                x = stocha.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, N_PATHS, seed=seed)
+                del x
+                x = stocha.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")],
+                                  STEPS, N_PATHS, seed=seed)
+                del x
+                x = stocha.merton_jump_diffusion(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j",
+                                                                       "sigma_j", "t")], STEPS, N_PATHS, seed=seed)
+                del x
+                return max_over_ranks(time.perf_counter() - t0)
+
+            # the first pass writes into fresh host memory; later passes reuse the
+            # host result cache's buffers, whose pages already exist
+            cold = e2e64_pass()
+            warm = min(e2e64_pass() for _ in range(2))
+            fp64["e2e"] = {"value": world * path_steps / warm, "unit": "path-steps/s",
+                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8 * N_PATHS * (STEPS + 1) * 5,
+                           "first_call_value": world * path_steps / cold}
         fp64["fp32_fused_speedup"] = value / fp64["value"]
 
     extras = {}

@@ -77,6 +77,25 @@ int stocha_ctx_set_stream(stocha_ctx* ctx, void* cuda_stream);
 int stocha_ctx_sync(stocha_ctx* ctx);
 const char* stocha_last_error(void);
 const char* stocha_version(void);
+
+/* ------------------------------------------------------ host result cache
+ * No counterpart in the reference (its functions return fresh NumPy arrays).
+ * Delivering a large result into fresh host memory is bound by faulting its
+ * pages in (~30 GB/s on a Grace host), while a copy into pages that already
+ * exist runs at the chip-to-chip link's rate (~190 GB/s on GB300, the same as
+ * pinned memory).  A binding that allocates its result arrays here gets back,
+ * for later results of a similar size, buffers whose pages already exist.
+ *   acquire: a buffer of at least `bytes` (page-aligned), a cached one of
+ *     capacity bytes..bytes*5/4 when there is one, else fresh memory.
+ *   release: hands a buffer from acquire back; it stays cached while the
+ *     cached total is within the cap, else the oldest are unmapped.
+ * The cap is STOCHA_HOST_CACHE_BYTES (bytes; 0 disables caching) or, by
+ * default, an eighth of physical memory up to 64 GiB.  The host-buffer calls
+ * (stocha_gbm, ...) skip the page population for a cached buffer. */
+int stocha_host_buffer_acquire(size_t bytes, void** out);
+int stocha_host_buffer_release(void* ptr);
+/* Bytes now cached (released and kept) and the cap; either pointer may be NULL. */
+int stocha_host_cache_stats(size_t* cached_bytes, size_t* cap_bytes);
 /* Diagnostic (no counterpart in the reference): the 256 integer thresholds
  * of the ziggurat fast path; (u >> 11) < thr[u & 0xFF] is the reference's
  * test  (u >> 11) * 2^-53 * X[L] < X[L+1]  (src/dist/normal.rs:25-27). */

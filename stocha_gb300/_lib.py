@@ -99,6 +99,9 @@ SIGNATURES = [
     ("stocha_ctx_sync", c_i32, [c_void_p]),
     ("stocha_last_error", c_char_p, []),
     ("stocha_version", c_char_p, []),
+    ("stocha_host_buffer_acquire", c_i32, [c_size, ctypes.POINTER(c_void_p)]),
+    ("stocha_host_buffer_release", c_i32, [c_void_p]),
+    ("stocha_host_cache_stats", c_i32, [ctypes.POINTER(c_size), ctypes.POINTER(c_size)]),
     ("stocha_gbm", c_i32, [c_void_p, c_dbl, c_dbl, c_dbl, c_dbl, c_u64, c_u64, c_u64, c_i32, c_dbl, P_dbl]),
     ("stocha_heston", c_i32, [c_void_p] + [c_dbl] * 8 + [c_u64, c_u64, c_u64, c_char_p, P_dbl]),
     ("stocha_merton_jump_diffusion", c_i32, [c_void_p] + [c_dbl] * 7 + [c_u64, c_u64, c_u64, P_dbl]),

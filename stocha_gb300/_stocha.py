@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes
 import operator
+import weakref
 
 import numpy as np
 
@@ -22,6 +23,30 @@ __version__ = "1.7.1"  # lib.rs:1879
 
 _U64_MAX = 2**64 - 1
 _U128_MAX = 2**128 - 1
+
+
+# --------------------------------------------------------- result arrays --
+_CACHE_MIN = 1 << 20  # smaller results go to plain NumPy memory
+
+
+def _release(addr):
+    load().stocha_host_buffer_release(ctypes.c_void_p(addr))
+
+
+def _host_array(shape, dtype=np.float64):
+    """A result array in the library's host-buffer cache: when it dies, its
+    pages (which exist by then) are kept for a later result of a similar size,
+    so that result's copy from the device skips the page faults of fresh memory
+    (stocha_host_buffer_acquire in stocha_gpu.h)."""
+    dt = np.dtype(dtype)
+    nbytes = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
+    if nbytes < _CACHE_MIN:
+        return np.empty(shape, dt)
+    p = ctypes.c_void_p()
+    check(load().stocha_host_buffer_acquire(nbytes, ctypes.byref(p)))
+    raw = (ctypes.c_char * nbytes).from_address(p.value)
+    weakref.finalize(raw, _release, p.value).atexit = False
+    return np.frombuffer(raw, dtype=dt).reshape(shape)
 
 
 # ---------------------------------------------------- PyO3-like conversion --
@@ -80,7 +105,7 @@ class RNG:
 
     def _fill(self, fn, size, *extra):
         size = _usize(size, "size")
-        out = np.empty(size, np.float64)
+        out = _host_array(size, np.float64)
         check(fn(None, ctypes.byref(self._st), size, *extra, dptr(out)))
         return out
 
@@ -96,7 +121,7 @@ class RNG:
     def raw_u64(self, size):
         """Raw generator words (no counterpart in the reference API)."""
         size = _usize(size, "size")
-        out = np.empty(size, np.uint64)
+        out = _host_array(size, np.uint64)
         check(load().stocha_rng_raw_u64(None, ctypes.byref(self._st), size, out.ctypes.data_as(_lib.P_u64)))
         return out
 
@@ -301,7 +326,7 @@ def _alloc(n_paths, cols, plausible, n_assets=None):
         shape = (0, 0) if n_assets is None else (0, 0, 0)
         return np.empty(shape, np.float64)
     shape = (n_paths, cols) if n_assets is None else (n_paths, cols, n_assets)
-    return np.empty(shape, np.float64)
+    return _host_array(shape, np.float64)
 
 
 # ------------------------------------------------------- exotic options ---
@@ -380,7 +405,7 @@ def gaussian_copula(corr, n_samples, seed=42):
     n_samples, seed = _usize(n_samples, "n_samples"), _usize(seed, "seed")
     c = np.ascontiguousarray(corr)
     rows, cols = c.shape
-    out = np.empty((n_samples, rows) if rows == cols else (0, 0), np.float64)
+    out = _host_array((n_samples, rows) if rows == cols else (0, 0), np.float64)
     check(load().stocha_gaussian_copula(None, dptr(c) if c.size else None, rows, cols, n_samples, seed,
                                         dptr(out) if out.size else None))
     return out
@@ -394,7 +419,7 @@ def student_t_copula(corr, nu, n_samples, seed=42):
     n_samples, seed = _usize(n_samples, "n_samples"), _usize(seed, "seed")
     c = np.ascontiguousarray(corr)
     rows, cols = c.shape
-    out = np.empty((n_samples, rows) if rows == cols and not nu <= 2.0 else (0, 0), np.float64)
+    out = _host_array((n_samples, rows) if rows == cols and not nu <= 2.0 else (0, 0), np.float64)
     check(load().stocha_student_t_copula(None, dptr(c) if c.size else None, rows, cols, nu, n_samples, seed,
                                          dptr(out) if out.size else None))
     return out

@@ -1,21 +1,28 @@
-// Device -> host delivery of large results into fresh pageable memory (the
-// NumPy arrays the reference's functions return).
+// Device -> host delivery of large results into pageable memory (the NumPy
+// arrays the reference's functions return).
 //
 // On a Grace host, a copy into host pages that already exist runs at the
-// chip-to-chip link's rate (~170 GB/s measured on GB300), but NumPy hands us
-// untouched virtual memory: the first write to each page faults it in and the
-// kernel zero-fills it, which a single-threaded copy does at 10-30 GB/s.  So
-// the destination's pages are populated by a small pool of host threads
-// (one write per page) while the GPU computes, and the copy is issued chunk
-// by chunk as chunks become ready.
+// chip-to-chip link's rate (~190 GB/s measured on GB300, the same as pinned
+// memory), but fresh memory is untouched virtual memory: the first write to
+// each page faults it in and the kernel zero-fills it, which a
+// single-threaded copy does at ~30 GB/s.  Two remedies:
+//   * the result cache (stocha_host_buffer_acquire/release) keeps released
+//     result buffers, whose pages exist, for later results of a similar size;
+//   * into fresh memory, the destination's pages are populated by a small
+//     pool of host threads (one write per page) and the copy is issued chunk
+//     by chunk as chunks become ready.
 #include <atomic>
 #include <condition_variable>
+#include <cstdlib>
+#include <deque>
 #include <functional>
 #include <memory>
 #include <mutex>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
+#include <sys/mman.h>
 #include <unistd.h>
 
 #include "host_common.h"
@@ -92,11 +99,117 @@ class HostPool {
   bool stop_ = false;
 };
 
+// Released result buffers, kept mapped (their pages exist) for reuse.
+class HostCache {
+ public:
+  static HostCache& get() {
+    static HostCache c;
+    return c;
+  }
+
+  void* acquire(size_t bytes) {
+    const size_t want = round_up(bytes ? bytes : 1);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      // best fit among the cached buffers of capacity want .. want * 5/4
+      size_t best = free_.size();
+      for (size_t i = 0; i < free_.size(); ++i) {
+        const size_t c = free_[i].cap;
+        if (c >= want && c - want <= want / 4 && (best == free_.size() || c < free_[best].cap)) best = i;
+      }
+      if (best != free_.size()) {
+        const Buf b = free_[best];
+        free_.erase(free_.begin() + (std::ptrdiff_t)best);
+        cached_ -= b.cap;
+        live_[b.p] = Live{b.cap, true};
+        return b.p;
+      }
+    }
+    void* p = mmap(nullptr, want, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
+    if (p == MAP_FAILED) return nullptr;
+    std::lock_guard<std::mutex> lk(mu_);
+    live_[p] = Live{want, false};
+    return p;
+  }
+
+  // false: not a buffer from acquire (or released twice)
+  bool release(void* p) {
+    std::vector<Buf> drop;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      auto it = live_.find(p);
+      if (it == live_.end()) return false;
+      const Buf b{p, it->second.cap};
+      const bool keep = it->second.populated && b.cap <= cap_;
+      live_.erase(it);
+      if (keep) {
+        free_.push_back(b);
+        cached_ += b.cap;
+        while (cached_ > cap_) {  // the oldest go first
+          drop.push_back(free_.front());
+          cached_ -= free_.front().cap;
+          free_.pop_front();
+        }
+      } else {
+        drop.push_back(b);
+      }
+    }
+    for (const Buf& b : drop) munmap(b.p, b.cap);
+    return true;
+  }
+
+  // Whether [dst, dst + bytes) lies in a handed-out buffer whose pages exist.
+  bool populated(const void* dst, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = live_.find(const_cast<void*>(dst));
+    return it != live_.end() && it->second.populated && bytes <= it->second.cap;
+  }
+  void mark_populated(const void* dst, size_t bytes) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = live_.find(const_cast<void*>(dst));
+    if (it != live_.end() && round_up(bytes) >= it->second.cap) it->second.populated = true;
+  }
+  void stats(size_t* cached, size_t* cap) {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (cached) *cached = cached_;
+    if (cap) *cap = cap_;
+  }
+
+ private:
+  struct Buf {
+    void* p;
+    size_t cap;
+  };
+  struct Live {
+    size_t cap;
+    bool populated;
+  };
+  HostCache() {
+    page_ = (size_t)sysconf(_SC_PAGESIZE);
+    const char* env = std::getenv("STOCHA_HOST_CACHE_BYTES");
+    if (env && *env) {
+      cap_ = (size_t)std::strtoull(env, nullptr, 10);
+    } else {
+      const size_t phys = (size_t)sysconf(_SC_PHYS_PAGES) * page_;
+      cap_ = phys / 8;
+      if (cap_ > (64ull << 30)) cap_ = 64ull << 30;
+    }
+  }
+  size_t round_up(size_t n) const { return (n + page_ - 1) / page_ * page_; }
+
+  std::mutex mu_;
+  std::deque<Buf> free_;
+  std::unordered_map<void*, Live> live_;
+  size_t cached_ = 0, cap_ = 0, page_ = 4096;
+};
+
 }  // namespace
 
 int copy_to_host_populated(cudaStream_t st, void* dst, const void* src, size_t bytes) {
-  if (bytes < kParallelMin) {
+  HostCache& cache = HostCache::get();
+  if (bytes < kParallelMin || cache.populated(dst, bytes)) {
     STOCHA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+    cache.mark_populated(dst, bytes);
     return STOCHA_OK;
   }
   HostPool& pool = HostPool::get();
@@ -126,7 +239,30 @@ int copy_to_host_populated(cudaStream_t st, void* dst, const void* src, size_t b
     if (e != cudaSuccess) rc = cuda_error(e, "cudaMemcpyAsync (device to host)");
   }
   pool.wait();  // the task's captures live on this frame
+  if (rc == STOCHA_OK) cache.mark_populated(dst, bytes);
   return rc;
 }
 
 }  // namespace stocha
+
+extern "C" {
+
+int stocha_host_buffer_acquire(size_t bytes, void** out) {
+  if (!out) return stocha::set_error(STOCHA_ERR_VALUE, "out must not be NULL");
+  *out = stocha::HostCache::get().acquire(bytes);
+  if (!*out) return stocha::set_error(STOCHA_ERR_NOMEM, "host buffer allocation failed");
+  return STOCHA_OK;
+}
+
+int stocha_host_buffer_release(void* ptr) {
+  if (!stocha::HostCache::get().release(ptr))
+    return stocha::set_error(STOCHA_ERR_VALUE, "not a buffer from stocha_host_buffer_acquire");
+  return STOCHA_OK;
+}
+
+int stocha_host_cache_stats(size_t* cached_bytes, size_t* cap_bytes) {
+  stocha::HostCache::get().stats(cached_bytes, cap_bytes);
+  return STOCHA_OK;
+}
+
+}  // extern "C"

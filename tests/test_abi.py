@@ -106,6 +106,37 @@ def test_conversion_errors(stocha):
         stocha.RNG(seed=2**128)
 
 
+def test_host_buffer_cache_host_logic(stocha):
+    """Acquire/release of the host result cache without a GPU: a buffer whose
+    pages were never written is unmapped on release (nothing cached), a
+    second release and a foreign pointer are errors, the cap is positive."""
+    import ctypes
+
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    cached, cap = ctypes.c_size_t(), ctypes.c_size_t()
+    _lib.check(lib.stocha_host_cache_stats(ctypes.byref(cached), ctypes.byref(cap)))
+    assert cap.value > 0
+    before = cached.value
+    p = ctypes.c_void_p()
+    _lib.check(lib.stocha_host_buffer_acquire(3 << 20, ctypes.byref(p)))
+    assert p.value and p.value % 4096 == 0
+    ctypes.memset(p.value, 7, 3 << 20)  # the memory is usable
+    _lib.check(lib.stocha_host_buffer_release(p))
+    _lib.check(lib.stocha_host_cache_stats(ctypes.byref(cached), None))
+    assert cached.value == before  # never filled by a device copy: not kept
+    for bad in (p, ctypes.c_void_p(12345)):
+        with pytest.raises(ValueError, match="not a buffer from stocha_host_buffer_acquire"):
+            _lib.check(lib.stocha_host_buffer_release(bad))
+    # the Python layer's arrays: small ones are plain NumPy memory, large ones cached buffers
+    small = stocha._stocha._host_array((10, 10))
+    big = stocha._stocha._host_array((1000, 253))
+    assert small.flags.owndata and not big.flags.owndata and big.flags.writeable and big.flags.c_contiguous
+    big[:] = 1.0
+    del big
+
+
 def test_rng_state_json_roundtrip(stocha):
     r = stocha.RNG(seed=2**100 + 7)
     assert r.seed == 2**100 + 7 and repr(r) == f"RNG(seed={2**100 + 7}, algorithm='pcg64dxsm')"

@@ -205,3 +205,34 @@ def test_table_exp_accuracy(stocha):
     assert np.isinf(y[x == 710.0]).all()
     sub = (want > 0) & (want < np.finfo(float).tiny)
     assert np.allclose(y[sub], want[sub], rtol=1e-12, atol=2 * np.spacing(0.0))
+
+
+def test_host_result_cache_reuse(stocha):
+    """A released result's buffer serves the next result of the same size: the
+    cached byte count rises on release and falls on reuse, and the values are
+    those of a fresh array."""
+    import ctypes
+    import gc
+
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+
+    def cached():
+        c = ctypes.c_size_t()
+        _lib.check(lib.stocha_host_cache_stats(ctypes.byref(c), None))
+        return c.value
+
+    kw = dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=252, n_paths=20_000, seed=3)
+    a = stocha.gbm(**kw)
+    first = a.copy()
+    base = cached()
+    del a
+    gc.collect()
+    assert cached() >= base + first.nbytes
+    b = stocha.gbm(**kw)
+    assert cached() <= base + 1
+    np.testing.assert_array_equal(b, first)
+    c = stocha.gbm(**dict(kw, seed=4))  # b is alive: a different buffer
+    assert not np.shares_memory(b, c) and not np.array_equal(b, c)
+
