@@ -46,6 +46,9 @@ struct stocha_ctx {
   double* h_small = nullptr;  // pinned, 4096 doubles for small results
   stocha::DevBuf out, partials, small, aux, starts;
   stocha::LsmcGraphs* lsmc_graphs = nullptr;  // LSMC sweep graphs for this context's stream
+  // overlap of materialised results' device-to-host copies with their compute
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t chunk_done[8] = {};
   std::recursive_mutex mu;
 };
 
@@ -99,6 +102,9 @@ int price_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, int precis
 // threads in the meantime and the copy goes out in chunks as they are ready
 // (hostcopy.cpp).  Returns after the last chunk is enqueued.
 int copy_to_host_populated(cudaStream_t st, void* dst, const void* src, size_t bytes);
+// Whether [dst, dst + bytes) is a host result-cache buffer whose pages exist
+// (a copy into it runs at the link's rate with no population pass).
+bool host_dst_cached(const void* dst, size_t bytes);
 // Enqueues a launch writing the terminal price of every path (FP64).
 int terminal_launch(stocha_ctx* c, const stocha_model* m, uint64_t seed, double* out_dev);
 

@@ -205,6 +205,8 @@ class HostCache {
 
 }  // namespace
 
+bool host_dst_cached(const void* dst, size_t bytes) { return HostCache::get().populated(dst, bytes); }
+
 int copy_to_host_populated(cudaStream_t st, void* dst, const void* src, size_t bytes) {
   HostCache& cache = HostCache::get();
   if (bytes < kParallelMin || cache.populated(dst, bytes)) {

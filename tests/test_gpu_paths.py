@@ -236,3 +236,28 @@ def test_host_result_cache_reuse(stocha):
     c = stocha.gbm(**dict(kw, seed=4))  # b is alive: a different buffer
     assert not np.shares_memory(b, c) and not np.array_equal(b, c)
 
+
+
+@pytest.mark.parametrize("antithetic", [False, True])
+def test_chunked_copy_overlap_same_result(stocha, antithetic):
+    """A large result copied into a cached host buffer is computed in row chunks
+    whose copies overlap the next chunk's compute; it must equal the one-launch
+    result (the first call, into fresh memory), row for row, including the
+    antithetic half and a multi-asset row layout."""
+    import gc
+
+    kw = dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=30, n_paths=700_001, seed=11, antithetic=antithetic)
+    a = stocha.gbm(**kw)  # > 64 MB, > 2^19 rows
+    first = a.copy()
+    del a
+    gc.collect()
+    b = stocha.gbm(**kw)  # into the cached buffer: the chunked form
+    np.testing.assert_array_equal(b, first)
+    del b, first
+    mk = dict(s0=[100.0, 50.0], mu=[0.05, 0.08], sigma=[0.2, 0.3], corr=np.array([[1.0, 0.6], [0.6, 1.0]]), t=1.0,
+              steps=20, n_paths=600_000, seed=5, antithetic=antithetic)
+    a = stocha.multi_gbm(**mk)
+    first = a.copy()
+    del a
+    gc.collect()
+    np.testing.assert_array_equal(stocha.multi_gbm(**mk), first)
