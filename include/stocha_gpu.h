@@ -101,7 +101,7 @@ int stocha_host_cache_stats(size_t* cached_bytes, size_t* cap_bytes);
  * test  (u >> 11) * 2^-53 * X[L] < X[L+1]  (src/dist/normal.rs:25-27). */
 int stocha_debug_zig_thresholds(uint64_t* thr256);
 /* Diagnostic (no counterpart in the reference): y[i] = exp(x[i]) by the
- * table-driven FP64 exponential the path kernels use (host buffers). */
+ * FP64 kernels' exponential, evaluated on the integer pipes (host buffers). */
 int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n);
 /* Diagnostic (no counterpart in the reference): measured peak rate of one
  * pipe for roofline denominators.  kind 0: FP32 FFMA flop/s, 1: FP64 DFMA
