@@ -34,7 +34,7 @@ extern "C" {
 #define STOCHA_ERR_BUSY 6     /* serving: admission refused (memory budget) */
 #define STOCHA_ERR_TIMEOUT 7  /* serving: a wait ended before the request finished */
 
-#define STOCHA_FP64 0 /* reference arithmetic, exact operation order */
+#define STOCHA_FP64 0 /* the reference's algorithm in FP64: paths within 1e-12 of its output */
 #define STOCHA_FP32 1 /* FP32 paths, FP64 reductions */
 
 #define STOCHA_MODEL_GBM 0
