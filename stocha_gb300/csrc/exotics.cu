@@ -136,13 +136,13 @@ __global__ void __launch_bounds__(128) k_exotic_f32(const __grid_constant__ Exot
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   unsigned err = 0;
   double sum = 0.0;
-  const float drift = (float)a.drift, diffusion = (float)a.diffusion, s0 = (float)a.s0, k = (float)a.k;
+  const float drift = a.f_drift, diffusion = a.f_diff, s0 = a.f_s0, k = a.f_k;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
     PcgGen g{pcg_path_state(a.ss, i), a.ss.inc_lo, a.ss.inc_hi};
     float ls = 0.0f;
     if (a.kind == kExoBarrier) {
-      const float lb = (float)a.lbarrier;
+      const float lb = a.f_lb;
       int hit = -1;
       if (a.already_hit) {
         hit = 0;
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(128) k_exotic_f32(const __grid_constant__ Exot
       const double rpv = a.rebate == 0.0 ? 0.0 : rebate_pv(a, hit);
       sum += (double)opt + rpv / a.discount;
     } else if (a.kind == kExoLookback) {
-      float lmx = (float)a.lm0, lmn = (float)a.ln0;
+      float lmx = a.f_lm0, lmn = a.f_ln0;
       for (uint64_t st = 0; st < a.steps; ++st) {
         ls += fmaf(diffusion, normal_f32(g, c, zs, err), drift);
         lmx = fmaxf(lmx, ls);
@@ -244,9 +244,19 @@ int exotic_grid(uint64_t n, int sms) {
 }
 
 void launch_exotic(const ExoticLaunch& a, int grid, cudaStream_t st) {
-  if (a.f32)
-    k_exotic_f32<<<grid, 128, 0, st>>>(a);
-  else
+  if (a.f32) {
+    // converted here rather than in the kernel, where the compiler may redo a
+    // conversion (an FP64-pipe instruction) inside the path loop
+    ExoticLaunch b = a;
+    b.f_drift = (float)a.drift;
+    b.f_diff = (float)a.diffusion;
+    b.f_s0 = (float)a.s0;
+    b.f_k = (float)a.k;
+    b.f_lb = (float)a.lbarrier;
+    b.f_lm0 = (float)a.lm0;
+    b.f_ln0 = (float)a.ln0;
+    k_exotic_f32<<<grid, 128, 0, st>>>(b);
+  } else
     k_exotic<<<grid, 128, 0, st>>>(a);
 }
 

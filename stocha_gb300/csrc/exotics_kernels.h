@@ -35,6 +35,8 @@ struct ExoticLaunch {
   double m0, n0;                  // lookback: initial running max / min
   double a_spent, w_spent, w_remain;  // seasoned Asian
   double lbarrier, lm0, ln0;          // FP32 form: ln(barrier / s0), ln(m0 / s0), ln(n0 / s0)
+  // FP32 form: the constants it reads, rounded once on the host (launch_exotic)
+  float f_drift, f_diff, f_s0, f_k, f_lb, f_lm0, f_ln0;
 };
 
 int exotic_grid(uint64_t n, int sms);

@@ -158,8 +158,11 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   unsigned err = 0;
-  const float s0 = (float)a.gbm.s0, drift = (float)a.gbm.drift, diffusion = (float)a.gbm.diffusion;
-  const float strike = (float)a.strike;
+  // FP32 constants rounded once on the host (F32K): under the register cap a
+  // value converted here from the double parameters could be rematerialised
+  // inside the path loop, putting a conversion on the FP64 pipe every step
+  const float s0 = a.f32.g_s0, drift = a.f32.g_drift, diffusion = a.f32.g_diff;
+  const float strike = a.f32.strike;
   // one path: materialised rows (kStore) or the payoff of S_T
   auto path = [&](uint64_t lrow, float* pay) {
     const uint64_t row = a.row_begin + lrow;
@@ -280,15 +283,18 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_eu
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
-  const HestonK& h = a.heston;
-  const float rho = (float)h.rho, rho_comp = (float)h.rho_comp, kappa_dt = (float)(h.kappa * h.dt);
-  const float theta = (float)h.theta, xi_sdt = (float)(h.xi * h.sqrt_dt), sdt = (float)h.sqrt_dt;
-  const float mu_dt = (float)(h.mu * h.dt), half_dt = (float)(0.5 * h.dt), s0 = (float)h.s0;
+  // FP32 constants rounded once on the host (F32K): converted here from the
+  // double parameters, the register cap made the compiler redo the DMUL and
+  // conversions inside the step loop (22 % of the FP64 pipe busy)
+  const F32K& f = a.f32;
+  const float rho = f.h_rho, rho_comp = f.h_rho_comp, kappa_dt = f.h_kdt;
+  const float theta = f.h_theta, xi_sdt = f.h_xsdt, sdt = f.h_sdt;
+  const float mu_dt = f.h_mudt, nhalf_dt = f.h_nhdt, s0 = f.h_s0;
   unsigned err = 0;
   auto path = [&](uint64_t lrow, float* pay) {
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
-    float v = (float)h.v0;
+    float v = f.h_v0;
     PathSum<kStore> lg;
     if (kStore) store32(a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
@@ -299,7 +305,7 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_eu
       float v_plus = fmaxf(v, 0.0f);
       float sqrt_v = sqrt_approx(v_plus);
       v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
-      lg.add(fmaf(-half_dt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
+      lg.add(fmaf(nhalf_dt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
       if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(lg.value()));
     }
     if (!kStore) pay[0] = payoff_f32(s0 * expf(lg.value()), a.f32.strike, a.payoff);
@@ -325,8 +331,9 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_merton_f3
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const MertonK& M = a.merton;
-  const float drift = (float)M.drift, diffusion = (float)M.diffusion, mu_j = (float)M.mu_j;
-  const float sigma_j = (float)M.sigma_j, s0 = (float)M.s0;
+  // FP32 constants rounded once on the host (F32K), not converted here
+  const float drift = a.f32.m_drift, diffusion = a.f32.m_diff, mu_j = a.f32.m_mu_j;
+  const float sigma_j = a.f32.m_sigma_j, s0 = a.f32.m_s0;
   unsigned err = 0;
   auto path = [&](uint64_t lrow, float* pay) {
     const uint64_t row = a.row_begin + lrow;
