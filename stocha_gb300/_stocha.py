@@ -30,7 +30,10 @@ _CACHE_MIN = 1 << 20  # smaller results go to plain NumPy memory
 
 
 def _release(addr):
-    load().stocha_host_buffer_release(ctypes.c_void_p(addr))
+    try:
+        load().stocha_host_buffer_release(ctypes.c_void_p(addr))
+    except Exception:  # interpreter shutdown: the process unmaps everything anyway
+        pass
 
 
 def _host_array(shape, dtype=np.float64):

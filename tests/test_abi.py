@@ -135,6 +135,27 @@ def test_host_buffer_cache_host_logic(stocha):
     assert small.flags.owndata and not big.flags.owndata and big.flags.writeable and big.flags.c_contiguous
     big[:] = 1.0
     del big
+    # concurrent acquire/release from several threads (the cache is process-wide)
+    import threading
+
+    errors = []
+
+    def work():
+        for _ in range(100):
+            q = ctypes.c_void_p()
+            if lib.stocha_host_buffer_acquire(2 << 20, ctypes.byref(q)) or not q.value:
+                errors.append("acquire")
+                return
+            ctypes.memset(q.value, 1, 4096)
+            if lib.stocha_host_buffer_release(q):
+                errors.append("release")
+
+    threads = [threading.Thread(target=work) for _ in range(8)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors
 
 
 def test_rng_state_json_roundtrip(stocha):
