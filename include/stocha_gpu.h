@@ -103,6 +103,9 @@ int stocha_debug_zig_thresholds(uint64_t* thr256);
 /* Diagnostic (no counterpart in the reference): y[i] = exp(x[i]) by the
  * FP64 kernels' exponential, evaluated on the integer pipes (host buffers). */
 int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n);
+/* Diagnostic (no counterpart in the reference): y[i] = sqrt(x[i]) by the FP64
+ * kernels' correctly rounded integer-pipe square root (host buffers). */
+int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n);
 /* Diagnostic (no counterpart in the reference): measured peak rate of one
  * pipe for roofline denominators.  kind 0: FP32 FFMA flop/s, 1: FP64 DFMA
  * flop/s, 2: 32-bit IMAD op/s, 3: PCG64DXSM draws/s (generator alone). */

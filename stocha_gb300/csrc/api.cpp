@@ -758,7 +758,7 @@ int stocha_autotune(stocha_ctx* ctx, const stocha_model* m, int32_t reps, stocha
   return STOCHA_OK;
 }
 
-int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n) {
+static int debug_f64(int fn, stocha_ctx* ctx, const double* x, double* y, uint64_t n) {
   int rc = resolve_ctx(&ctx);
   if (rc) return rc;
   if (n == 0) return STOCHA_OK;
@@ -768,11 +768,15 @@ int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n) {
   double* d = (double*)ctx->aux.ptr;
   if ((rc = begin_call(ctx))) return rc;
   STOCHA_CUDA(cudaMemcpyAsync(d, x, n * 8, cudaMemcpyHostToDevice, ctx->stream));
-  launch_debug_exp(d, d + n, n, ctx->d_tabs, ctx->stream);
+  launch_debug_f64(fn, d, d + n, n, ctx->d_tabs, ctx->stream);
   STOCHA_CUDA(cudaGetLastError());
   STOCHA_CUDA(cudaMemcpyAsync(y, d + n, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
   return finish_call(ctx);
 }
+
+int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n) { return debug_f64(0, ctx, x, y, n); }
+
+int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n) { return debug_f64(1, ctx, x, y, n); }
 
 int stocha_debug_zig_thresholds(uint64_t* thr256) {
   ZigTables t;

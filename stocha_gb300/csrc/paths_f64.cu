@@ -162,8 +162,8 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
         double dw1 = normal_f64(s, c, zs, err);
         double dz = normal_f64(s, c, zs, err);
         double dw2 = h.rho * dw1 + h.rho_comp * dz;
-        double v_plus = fmax(v, 0.0);
-        double sqrt_v = sqrt(v_plus);
+        const double v_plus = max0_int(v);
+        const double sqrt_v = sqrt_rn_int(v_plus);  // the same double as sqrt()
         // the variance recursion keeps the reference's operations and roundings
         // (it feeds back through fmax(v, 0)); the log-price increment
         // (mu - v+/2) dt + sqrt(v+ dt) dW1 only feeds x, so it is fused
@@ -272,12 +272,13 @@ __global__ void __launch_bounds__(128) k_hull_white_f64(const __grid_constant__ 
   if (err) atomicOr(a.err, err);
 }
 
-__global__ void k_debug_exp(const double* __restrict__ x, double* __restrict__ y, uint64_t n,
+// fn 0: the kernels' exponential, 1: their correctly rounded sqrt
+__global__ void k_debug_f64(int fn, const double* __restrict__ x, double* __restrict__ y, uint64_t n,
                             const ZigTables* tabs) {
   __shared__ ZigShared zs;
   zig_stage(zs, tabs, true);
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-    y[i] = mul_exp(1.0, x[i], zs);
+    y[i] = fn == 0 ? mul_exp(1.0, x[i], zs) : sqrt_rn_int(x[i]);
 }
 
 // Block v sums value v of all records: thread t adds records t, t + 256, ...
@@ -355,8 +356,8 @@ int launch_paths_f64(const PathLaunch& L, cudaStream_t st) {
   return cudaPeekAtLastError() == cudaSuccess ? g : -1;
 }
 
-void launch_debug_exp(const double* x, double* y, uint64_t n, const ZigTables* tabs, cudaStream_t st) {
-  k_debug_exp<<<256, 256, 0, st>>>(x, y, n, tabs);
+void launch_debug_f64(int fn, const double* x, double* y, uint64_t n, const ZigTables* tabs, cudaStream_t st) {
+  k_debug_f64<<<256, 256, 0, st>>>(fn, x, y, n, tabs);
 }
 
 void launch_reduce_partials(const double* partials, int nblocks, int nvals, double* out, cudaStream_t st) {

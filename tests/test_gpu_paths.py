@@ -207,6 +207,35 @@ def test_table_exp_accuracy(stocha):
     assert np.allclose(y[sub], want[sub], rtol=1e-12, atol=2 * np.spacing(0.0))
 
 
+def test_integer_sqrt_is_correctly_rounded(stocha):
+    """The FP64 kernels' integer-pipe square root (Heston's variance recursion)
+    returns exactly IEEE sqrt's double, which the reference's f64::sqrt returns:
+    random values over the whole exponent range and the working range,
+    perfect squares and their neighbours, and the special values."""
+    import ctypes
+
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(19)
+    k = rng.integers(1, 2**26, 200_000).astype(np.float64)
+    sq = k * k * np.ldexp(1.0, rng.integers(-60, 60, k.size))
+    x = np.concatenate([
+        rng.uniform(0.0, 0.2, 500_000),
+        np.ldexp(rng.uniform(0.5, 1.0, 500_000), rng.integers(-1021, 1023, 500_000)),
+        sq, np.nextafter(sq, 0.0), np.nextafter(sq, np.inf),
+        [0.0, -0.0, 1.0, 2.0, 4.0, 0.25, np.finfo(float).tiny, np.finfo(float).max, 5e-324, 1e-310,
+         np.inf, -1.0, np.nan],
+    ])
+    y = np.empty_like(x)
+    P = ctypes.POINTER(ctypes.c_double)
+    _lib.check(lib.stocha_debug_sqrt(None, x.ctypes.data_as(P), y.ctypes.data_as(P), x.size))
+    with np.errstate(invalid="ignore"):
+        want = np.sqrt(x)
+    assert np.array_equal(y.view(np.uint64)[~np.isnan(want)], want.view(np.uint64)[~np.isnan(want)])
+    assert np.isnan(y[np.isnan(want)]).all()
+
+
 def test_host_result_cache_reuse(stocha):
     """A released result's buffer serves the next result of the same size: the
     cached byte count rises on release and falls on reuse, and the values are
