@@ -152,6 +152,7 @@ SIGNATURES = [
     ("stocha_debug_zig_thresholds", c_i32, [P_u64]),
     ("stocha_debug_exp", c_i32, [c_void_p, P_dbl, P_dbl, c_u64]),
     ("stocha_debug_sqrt", c_i32, [c_void_p, P_dbl, P_dbl, c_u64]),
+    ("stocha_debug_f64", c_i32, [c_void_p, c_i32, P_dbl, P_dbl, c_u64]),
     ("stocha_measure_peak", c_i32, [c_void_p, c_i32, P_dbl]),
 ]
 

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
 #pragma unroll
-      for (int i = 0; i < na; ++i) z[i] = normal_f64(s, c, zs, err);
+      for (int i = 0; i < na; ++i) z[i] = normal_f64<true>(s, c, zs, err);  // FP64-pipe bound: integer products
 #pragma unroll
       for (int i = 0; i < na; ++i) {
         // row i of L z, one rounding per term
@@ -159,8 +159,8 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
       const double mu_dt = h.mu * h.dt, nhalf_dt = -0.5 * h.dt;
 #pragma unroll 1
       for (uint64_t k = 1; k <= a.steps; ++k) {
-        double dw1 = normal_f64(s, c, zs, err);
-        double dz = normal_f64(s, c, zs, err);
+        const double dw1 = normal_f64<true>(s, c, zs, err);  // FP64-pipe bound: integer products
+        const double dz = normal_f64<true>(s, c, zs, err);
         double dw2 = h.rho * dw1 + h.rho_comp * dz;
         const double v_plus = max0_int(v);
         const double sqrt_v = sqrt_rn_int(v_plus);  // the same double as sqrt()
@@ -272,13 +272,18 @@ __global__ void __launch_bounds__(128) k_hull_white_f64(const __grid_constant__ 
   if (err) atomicOr(a.err, err);
 }
 
-// fn 0: the kernels' exponential, 1: their correctly rounded sqrt
+// fn 0: the kernels' exponential, 1: their correctly rounded sqrt, 2 and 3:
+// the normal's product m * X[L] 2^-53 (L = i mod 256) on the integer pipes and
+// by DMUL
 __global__ void k_debug_f64(int fn, const double* __restrict__ x, double* __restrict__ y, uint64_t n,
                             const ZigTables* tabs) {
   __shared__ ZigShared zs;
   zig_stage(zs, tabs, true);
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-    y[i] = fn == 0 ? mul_exp(1.0, x[i], zs) : sqrt_rn_int(x[i]);
+    y[i] = fn == 0   ? mul_exp(1.0, x[i], zs)
+           : fn == 1 ? sqrt_rn_int(x[i])
+           : fn == 2 ? mul_u53_rn((uint64_t)x[i], zs.xs[i & 255])
+                     : __dmul_rn(x[i], zs.xs[i & 255]);
 }
 
 // Block v sums value v of all records: thread t adds records t, t + 256, ...

@@ -236,6 +236,33 @@ def test_integer_sqrt_is_correctly_rounded(stocha):
     assert np.isnan(y[np.isnan(want)]).all()
 
 
+def test_integer_normal_product_equals_dmul(stocha):
+    """The normal's product (u >> 11) * X[L] 2^-53 on the integer pipes (used by
+    the FP64-pipe-bound multi-GBM and Heston kernels) equals the FP64 pipe's
+    correctly rounded DMUL bit for bit, over every layer and the whole 53-bit
+    range, including 0, 1 and 2^53 - 1."""
+    import ctypes
+
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(23)
+    n = 256 * 4000
+    m = rng.integers(0, 2**53, n, dtype=np.uint64)
+    m[::7] >>= rng.integers(1, 52, m[::7].size).astype(np.uint64)
+    m[:256] = 0
+    m[256:512] = 1
+    m[512:768] = 2**53 - 1
+    x = m.astype(np.float64)
+    assert (x.astype(np.uint64) == m).all()
+    y_int, y_fp = np.empty_like(x), np.empty_like(x)
+    P = ctypes.POINTER(ctypes.c_double)
+    _lib.check(lib.stocha_debug_f64(None, 2, x.ctypes.data_as(P), y_int.ctypes.data_as(P), n))
+    _lib.check(lib.stocha_debug_f64(None, 3, x.ctypes.data_as(P), y_fp.ctypes.data_as(P), n))
+    assert np.array_equal(y_int.view(np.uint64), y_fp.view(np.uint64))
+    assert (y_fp[:256] == 0).all() and (y_fp[256:] >= 0).all()
+
+
 def test_host_result_cache_reuse(stocha):
     """A released result's buffer serves the next result of the same size: the
     cached byte count rises on release and falls on reuse, and the values are
