@@ -317,3 +317,24 @@ def test_chunked_copy_overlap_same_result(stocha, antithetic):
     del a
     gc.collect()
     np.testing.assert_array_equal(stocha.multi_gbm(**mk), first)
+
+
+@pytest.mark.parametrize("model", ["heston", "heston_qe", "merton", "hull_white"])
+def test_chunked_copy_overlap_other_models(stocha, model):
+    """The chunked copy/compute overlap for every other materialising model:
+    second call (cached buffer, row chunks) equals the first (one launch)."""
+    import gc
+
+    calls = {
+        "heston": lambda: stocha.heston(100.0, 0.04, 0.05, 2.0, 0.04, 0.3, -0.7, 1.0, 24, 560_001, seed=9),
+        "heston_qe": lambda: stocha.heston(100.0, 0.04, 0.05, 2.0, 0.04, 0.3, -0.7, 1.0, 24, 560_001, seed=9,
+                                           scheme="qe"),
+        "merton": lambda: stocha.merton_jump_diffusion(100.0, 0.05, 0.2, 1.0, -0.05, 0.1, 1.0, 24, 560_001, seed=9),
+        "hull_white": lambda: stocha.hull_white(0.03, 0.1, 0.005, 0.01, 1.0, 24, 560_001, seed=9),
+    }
+    a = calls[model]()
+    assert a.nbytes >= 64 << 20
+    first = a.copy()
+    del a
+    gc.collect()
+    np.testing.assert_array_equal(calls[model](), first)
