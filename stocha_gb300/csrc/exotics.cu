@@ -73,8 +73,9 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
         }
       const double opt = a.kind_in ? (knocked ? intrinsic(s, a.k, a.is_call) : 0.0)
                                    : (knocked ? 0.0 : intrinsic(s, a.k, a.is_call));
-      const double rpv = a.rebate == 0.0 ? 0.0 : rebate_pv(a, hit);
-      sum += opt + rpv / a.discount;
+      // no rebate (the common case, uniform over the launch): opt + 0 / discount
+      // is opt, without the FP64 division
+      sum += a.rebate == 0.0 ? opt : opt + rebate_pv(a, hit) / a.discount;
     } else if (a.kind == kExoLookback) {
       double mx = a.m0, mn = a.n0;
       for (uint64_t st = 0; st < a.steps; ++st) {
@@ -161,8 +162,7 @@ __global__ void __launch_bounds__(128) k_exotic_f32(const __grid_constant__ Exot
       const float sT = s0 * expf(ls);
       const float iv = a.is_call ? fmaxf(sT - k, 0.0f) : fmaxf(k - sT, 0.0f);
       const float opt = a.kind_in ? (knocked ? iv : 0.0f) : (knocked ? 0.0f : iv);
-      const double rpv = a.rebate == 0.0 ? 0.0 : rebate_pv(a, hit);
-      sum += (double)opt + rpv / a.discount;
+      sum += a.rebate == 0.0 ? (double)opt : (double)opt + rebate_pv(a, hit) / a.discount;
     } else if (a.kind == kExoLookback) {
       float lmx = a.f_lm0, lmn = a.f_ln0;
       for (uint64_t st = 0; st < a.steps; ++st) {
