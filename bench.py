@@ -72,6 +72,16 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
+def hbm_peak_gbs():
+    """Measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json,
+    written per machine), else the fallback 6800 GB/s."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        return 6800.0, "fallback"
+
+
 class ClockSampler:
     """nvidia-smi SM clock / throttle reasons sampled during the timed region."""
 
@@ -676,6 +686,11 @@ def run_ours(args, rank, world):
                            "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8 * N_PATHS * (STEPS + 1) * 5,
                            "first_call_value": world * path_steps / cold}
         fp64["fp32_fused_speedup"] = value / fp64["value"]
+        hbm, hbm_src = hbm_peak_gbs()
+        gbs = fp64["bytes_written_per_step"] / (ms64 * 1e-3) / 1e9
+        fp64["roofline"] = {"bound": "FP64 pipe (Heston) and issue (the others); not HBM, see profiles/",
+                            "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
+                            "peak_source": hbm_src, "note": "algorithmic bytes = the materialised paths written"}
         fp64["form"] = ("reference algorithm in FP64 (paths within 1e-12 of the oracle); its exponential, the "
                         "Heston sqrt and the normals' products run on the integer pipes (GB300 issues FP64 at "
                         "1/64 of FP32), 2.7x the FP64-pipe form against which the FP32 fused form was 9.7x")
@@ -711,6 +726,9 @@ def run_ours(args, rank, world):
                          # (ncu, profiles/k_gbm_uf3_fused_200k.md): the staged ziggurat tables only,
                          # the same at any path count (no path data leaves the registers)
                          "traffic": 77824, "traffic_unit": "bytes per launch (multi-GBM kernel)",
+                         # that traffic over the kernel's time, against the measured HBM rate: the
+                         # fused form is not memory-bound
+                         "hbm_frac": 77824 / (per_model["multi_gbm"] * 1e-3) / (hbm_peak_gbs()[0] * 1e9),
                          "kernel_ms": per_model, "peak_source": "measured live (stocha_measure_peak kind 3)"},
             "fp64_plain": fp64,
             "autotune": tuning,
