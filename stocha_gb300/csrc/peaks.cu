@@ -1,5 +1,6 @@
-// Peak-rate microbenchmarks for the roofline denominators the driver does not
-// measure (MEASURED_PEAKS.json holds HBM and bf16 tensor rates only):
+// Peak-rate microbenchmarks for the roofline denominators of pipes that a copy
+// or GEMM benchmark does not measure (the machine's measured peaks cover HBM
+// copy bandwidth and bf16 tensor throughput only):
 //   0  FP32 FFMA        (independent chains, ops = 2 flop each)
 //   1  FP64 DFMA
 //   2  32-bit IMAD
