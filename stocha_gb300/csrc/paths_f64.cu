@@ -74,8 +74,23 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
     const double drift = a.gbm.drift, diffusion = neg ? -a.gbm.diffusion : a.gbm.diffusion;
     double x = a.gbm.s0;
     if (kStore) store64(a, lrow, 0, 1, 0, x);
+    // Two steps at a time: both draws, then both exponentials (independent
+    // chains the compiler interleaves), then the two dependent products.  At
+    // small path counts a warp's step is latency-bound on the exponential's
+    // chain; the values are those of the one-step loop.
+    uint64_t k = 1;
 #pragma unroll 1
-    for (uint64_t k = 1; k <= a.steps; ++k) {
+    for (; k + 1 <= a.steps; k += 2) {
+      const double z0 = normal_f64(s, c, zs, err);
+      const double z1 = normal_f64(s, c, zs, err);
+      const double y0 = exp_y(fma(diffusion, z0, drift), zs);
+      const double y1 = exp_y(fma(diffusion, z1, drift), zs);
+      x *= y0;
+      if (kStore) store64(a, lrow, k, 1, 0, x);
+      x *= y1;
+      if (kStore) store64(a, lrow, k + 1, 1, 0, x);
+    }
+    if (k <= a.steps) {
       const double z = normal_f64(s, c, zs, err);
       x = mul_exp(x, fma(diffusion, z, drift), zs);
       if (kStore) store64(a, lrow, k, 1, 0, x);
