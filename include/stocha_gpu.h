@@ -109,7 +109,8 @@ int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n);
 /* Diagnostic (no counterpart in the reference): the FP64 kernels' helpers by
  * number: 0 exp (as stocha_debug_exp), 1 sqrt (as stocha_debug_sqrt), 2 the
  * normal's product (uint64)x[i] * X[L] 2^-53 with L = i mod 256 on the integer
- * pipes, 3 the same product by the FP64 pipe (they must agree bit for bit). */
+ * pipes, 3 the same product by the FP64 pipe (they must agree bit for bit),
+ * 4 exp in the early-exit form (bit for bit the same as 0). */
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n);
 /* Diagnostic (no counterpart in the reference): measured peak rate of one
  * pipe for roofline denominators.  kind 0: FP32 FFMA flop/s, 1: FP64 DFMA

@@ -779,7 +779,7 @@ int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n) { 
 int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n) { return debug_f64(1, ctx, x, y, n); }
 
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n) {
-  if (fn < 0 || fn > 3) return set_error(STOCHA_ERR_VALUE, "fn must be 0..3");
+  if (fn < 0 || fn > 4) return set_error(STOCHA_ERR_VALUE, "fn must be 0..4");
   return debug_f64(fn, ctx, x, y, n);
 }
 

@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       } else {
         for (uint64_t st = 1; st <= a.steps; ++st) {
           const double z = normal_f64(g, c, zs, err);
-          s = mul_exp(s, fma(a.diffusion, z, a.drift), zs);
+          s = mul_exp<false>(s, fma(a.diffusion, z, a.drift), zs);
           // s > 0 and the barrier is validated positive
           if (a.direction == 0 ? ge_pos(s, a.barrier) : ge_pos(a.barrier, s)) {
             hit = (int)st;
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       if (knocked && a.kind_in && (uint64_t)hit < a.steps)  // drive a knocked-in path to T
         for (uint64_t st = (uint64_t)hit; st < a.steps; ++st) {
           const double z = normal_f64(g, c, zs, err);
-          s = mul_exp(s, fma(a.diffusion, z, a.drift), zs);
+          s = mul_exp<false>(s, fma(a.diffusion, z, a.drift), zs);
         }
       const double opt = a.kind_in ? (knocked ? intrinsic(s, a.k, a.is_call) : 0.0)
                                    : (knocked ? 0.0 : intrinsic(s, a.k, a.is_call));
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       double mx = a.m0, mn = a.n0;
       for (uint64_t st = 0; st < a.steps; ++st) {
         const double z = normal_f64(g, c, zs, err);
-        s = mul_exp(s, fma(a.diffusion, z, a.drift), zs);
+        s = mul_exp<false>(s, fma(a.diffusion, z, a.drift), zs);
         // s > 0 and mx >= s0 > 0; mn may be any non-NaN value
         if (!ge_pos(mx, s)) mx = s;
         if (!ge_pos(s, mn)) mn = s;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       for (uint64_t st = 0; st < a.steps; ++st) {
         const double z = normal_f64(g, c, zs, err);
         const double x = fma(a.diffusion, z, a.drift);
-        s = mul_exp(s, x, zs);
+        s = mul_exp<false>(s, x, zs);
         lg += x;
         sum_arith += s;
         sum_log += lg;

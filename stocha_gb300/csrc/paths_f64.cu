@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
         const double z_j = normal_f64(s, c, zs, err);
         ret += fma(M.sigma_j, z_j, M.mu_j);
       }
-      x = mul_exp(x, ret, zs);
+      x = mul_exp<false>(x, ret, zs);  // issue-bound: the early-exit form
       if (kStore) store64(a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
@@ -289,7 +289,7 @@ __global__ void __launch_bounds__(128) k_hull_white_f64(const __grid_constant__ 
 
 // fn 0: the kernels' exponential, 1: their correctly rounded sqrt, 2 and 3:
 // the normal's product m * X[L] 2^-53 (L = i mod 256) on the integer pipes and
-// by DMUL
+// by DMUL, 4: the exponential's early-exit form
 __global__ void k_debug_f64(int fn, const double* __restrict__ x, double* __restrict__ y, uint64_t n,
                             const ZigTables* tabs) {
   __shared__ ZigShared zs;
@@ -298,7 +298,8 @@ __global__ void k_debug_f64(int fn, const double* __restrict__ x, double* __rest
     y[i] = fn == 0   ? mul_exp(1.0, x[i], zs)
            : fn == 1 ? sqrt_rn_int(x[i])
            : fn == 2 ? mul_u53_rn((uint64_t)x[i], zs.xs[i & 255])
-                     : __dmul_rn(x[i], zs.xs[i & 255]);
+           : fn == 3 ? __dmul_rn(x[i], zs.xs[i & 255])
+                     : mul_exp<false>(1.0, x[i], zs);
 }
 
 // Block v sums value v of all records: thread t adds records t, t + 256, ...
