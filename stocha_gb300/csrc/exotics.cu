@@ -88,16 +88,19 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
       sum += a.strike_fixed ? (a.is_call ? fmax(mx - a.k, 0.0) : fmax(a.k - mn, 0.0))
                             : (a.is_call ? s - mn : mx - s);
     } else {  // Asian: plain (per-path pair) or floating seasoned (block sum)
-      double sum_arith = 0.0, sum_log = 0.0, lg = a.log_s0;
+      // sum over steps of ln s_k = n ln s0 + sum_i (n - i + 1) x_i: one DFMA a
+      // step with the integer weight built on the integer pipes, instead of the
+      // running log and its running sum (two DADDs)
+      double sum_arith = 0.0, sum_wx = 0.0;
       for (uint64_t st = 0; st < a.steps; ++st) {
         const double z = normal_f64(g, c, zs, err);
         const double x = fma(a.diffusion, z, a.drift);
         s = mul_exp<false>(s, x, zs);
-        lg += x;
         sum_arith += s;
-        sum_log += lg;
+        sum_wx = fma(u53_scaled_f64(a.steps - st, 0), x, sum_wx);
       }
       const double nsteps = (double)a.steps;
+      const double sum_log = fma(nsteps, a.log_s0, sum_wx);
       const double avg_a = sum_arith / nsteps;
       const double avg_g = exp(sum_log / nsteps);
       if (a.kind == kExoAsian) {
