@@ -70,6 +70,10 @@ struct PathLaunch {
   // which the launcher zeroes, and write one partial record per batch
   unsigned long long* work;
   uint32_t batch_rows;
+  // fused mode: when non-zero, the launcher returns kRecordsExceeded without
+  // launching if its grid would write more partial records than this (callers
+  // whose record buffer has a fixed size)
+  uint64_t max_records;
   double strike;
   int payoff;
   double aux[4];  // payoff parameters (pathwise estimators: s0, r, sigma, t)
@@ -98,12 +102,24 @@ int tune_slot(int model, int na);  // -1: no fused FP32 kernel for this model
 FusedTune get_fused_tune(int slot);
 int set_fused_tune(int slot, FusedTune t);  // 0, or -1 for an invalid slot or shape
 
+// Whether the staged sector writer takes L's rows: row-major output of at
+// least two 32-byte sectors a row (the first and last sectors of a row are
+// then distinct) and below 2^31 elements (its offsets are 32-bit).
+inline bool row_store_fits(const PathLaunch& L, uint64_t elem) {
+  if (L.time_major || L.terminal_only) return false;
+  const uint64_t width = L.model == kMultiGbm ? (uint64_t)L.multi.na : 1;
+  const uint64_t row_len = (L.steps + 1) * width;
+  return row_len >= 2 * (32 / elem) && row_len < (1ull << 31);
+}
+
 // Rounds the FP32 constants of L (after the model constants are set).
 void fill_f32_constants(PathLaunch* L);
 
 // Launch helpers (paths_f64.cu / paths_f32.cu).  Return the number of
 // partial records written in fused mode (blocks launched, or batches in the
-// work-queue mode), or -1 on error.
+// work-queue mode), -1 on error, or kRecordsExceeded (nothing launched) when
+// that number would exceed L.max_records.
+constexpr int kRecordsExceeded = -2;
 int launch_paths_f64(const PathLaunch& L, cudaStream_t st);
 int launch_paths_f32(const PathLaunch& L, cudaStream_t st);
 // y[i] = exp(x[i]) by the kernels' table-driven exponential (diagnostic).

@@ -18,9 +18,14 @@
 #include "engine.h"
 #include "mc_device.cuh"
 #include "reduce.cuh"
+#include "row_store.cuh"
 
 namespace stocha {
 namespace {
+
+// Staging area of the row-major stores: RowStore<float>::bytes(blockDim.x)
+// bytes, passed at launch in the kRows mode.
+extern __shared__ __align__(16) unsigned char dyn_smem[];
 
 struct Kahan {
   float s = 0.0f, c = 0.0f;
@@ -68,6 +73,15 @@ __device__ __forceinline__ void store32(const PathLaunch& a, uint64_t lrow, uint
     a.out_f32[(step * width + col) * a.rows + lrow] = v;
   else
     a.out_f32[(lrow * (a.steps + 1) + step) * width + col] = v;
+}
+
+template <int kMode>
+__device__ __forceinline__ void emit32(PathOut<float, kMode>& out, const PathLaunch& a, uint64_t lrow, uint64_t step,
+                                       uint64_t width, uint64_t col, float v) {
+  if (kMode == kRows)
+    out.rs.put(v);
+  else if (kMode == kElems)
+    store32(a, lrow, step, width, col, v);
 }
 
 // Block partial record: {sum payoff, sum payoff^2} per asset, compensated
@@ -152,8 +166,11 @@ __device__ __forceinline__ void run_rows(const PathLaunch& a, Batch&& batch) {
   store_partials<NV>(a, acc, acc2);
 }
 
-template <bool kStore>
+template <int kMode>
 __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
+  PathOut<float, kMode> out;
+  out.init(dyn_smem);
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -170,14 +187,15 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
     PathSum<kStore> w;
     float kf = 0.0f;  // step count as float (no per-step integer conversion)
-    if (kStore) store32(a, lrow, 0, 1, 0, s0);
+    if (kMode == kRows) out.begin(a.out_f32 + lrow * (a.steps + 1));
+    if (kStore) emit32(out, a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       float z = normal_f32(s, c, zs, err);
       if (kStore) {
         w.add(neg ? -z : z);
         kf += 1.0f;
-        store32(a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value())));
+        emit32(out, a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value())));
       } else {
         w.add(z);  // the antithetic sign is applied to the sum (negation is exact)
       }
@@ -188,9 +206,7 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
     }
   };
   if constexpr (kStore) {
-    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads)
-      path(lrow, nullptr);
+    for_rows(a.rows, out, [&](uint64_t lrow) { path(lrow, nullptr); });
   } else {
     run_rows<1>(a, [&](uint64_t b, float* p) {
       const uint64_t lrow = b + (threadIdx.x & 31u);
@@ -202,8 +218,11 @@ __global__ void __launch_bounds__(256) k_gbm_f32(const __grid_constant__ PathLau
   if (err) atomicOr(a.err, err);
 }
 
-template <int NA, bool kStore>
-__global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm_f32(const __grid_constant__ PathLaunch a) {
+template <int NA, int kMode>
+__global__ void __launch_bounds__(256, kMode != kFused ? 1 : kFusedMinBlocks) k_multi_gbm_f32(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
+  PathOut<float, kMode> out;
+  out.init(dyn_smem);
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -217,8 +236,9 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
     PathSum<kStore> w[CAP];
     float kf = 0.0f;
+    if (kMode == kRows) out.begin(a.out_f32 + lrow * (a.steps + 1) * na);
     if (kStore)
-      for (int i = 0; i < na; ++i) store32(a, lrow, 0, na, i, f.a_s0[i]);
+      for (int i = 0; i < na; ++i) emit32(out, a, lrow, 0, na, i, f.a_s0[i]);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
 #pragma unroll
@@ -234,7 +254,7 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm
 #pragma unroll
           for (int m = 0; m <= i; ++m) eps = fmaf(f.a_L[i * kMaxAssets + m], w[m].value(), eps);
           float lg = fmaf(kf, f.a_drift[i], f.a_diff[i] * eps);
-          store32(a, lrow, k, na, i, f.a_s0[i] * expf(lg));
+          emit32(out, a, lrow, k, na, i, f.a_s0[i] * expf(lg));
         }
       }
     }
@@ -260,8 +280,7 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm
     // materialised rows, or the fused form for more than 4 assets (static,
     // one record of na assets per block)
     Kahan acc[CAP], acc2[CAP];
-    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+    for_rows(a.rows, out, [&](uint64_t lrow) {
       float p[CAP];
       path(lrow, p);
       if (!kStore)
@@ -269,7 +288,7 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm
           acc[i].add(p[i]);
           acc2[i].add(p[i] * p[i]);
         }
-    }
+    });
     if (!kStore)
       for (int i = 0; i < na; ++i)
         block_sum2_store((double)acc[i].value(), (double)acc2[i].value(),
@@ -278,8 +297,11 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_multi_gbm
   if (err) atomicOr(a.err, err);
 }
 
-template <bool kStore>
-__global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_euler_f32(const __grid_constant__ PathLaunch a) {
+template <int kMode>
+__global__ void __launch_bounds__(256, kMode != kFused ? 1 : kFusedMinBlocks) k_heston_euler_f32(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
+  PathOut<float, kMode> out;
+  out.init(dyn_smem);
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -296,7 +318,8 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_eu
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     float v = f.h_v0;
     PathSum<kStore> lg;
-    if (kStore) store32(a, lrow, 0, 1, 0, s0);
+    if (kMode == kRows) out.begin(a.out_f32 + lrow * (a.steps + 1));
+    if (kStore) emit32(out, a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       float dw1 = normal_f32(s, c, zs, err);
@@ -306,14 +329,12 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_eu
       float sqrt_v = sqrt_approx(v_plus);
       v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
       lg.add(fmaf(nhalf_dt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(lg.value()));
+      if (kStore) emit32(out, a, lrow, k, 1, 0, s0 * expf(lg.value()));
     }
     if (!kStore) pay[0] = payoff_f32(s0 * expf(lg.value()), a.f32.strike, a.payoff);
   };
   if constexpr (kStore) {
-    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads)
-      path(lrow, nullptr);
+    for_rows(a.rows, out, [&](uint64_t lrow) { path(lrow, nullptr); });
   } else {
     run_rows<1>(a, [&](uint64_t b, float* p) {
       const uint64_t lrow = b + (threadIdx.x & 31u);
@@ -325,8 +346,11 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_heston_eu
   if (err) atomicOr(a.err, err);
 }
 
-template <bool kStore>
-__global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_merton_f32(const __grid_constant__ PathLaunch a) {
+template <int kMode>
+__global__ void __launch_bounds__(256, kMode != kFused ? 1 : kFusedMinBlocks) k_merton_f32(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
+  PathOut<float, kMode> out;
+  out.init(dyn_smem);
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -340,22 +364,21 @@ __global__ void __launch_bounds__(256, kStore ? 1 : kFusedMinBlocks) k_merton_f3
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     PathSum<kStore> w;
     float jumps = 0.0f, kf = 0.0f;
-    if (kStore) store32(a, lrow, 0, 1, 0, s0);
+    if (kMode == kRows) out.begin(a.out_f32 + lrow * (a.steps + 1));
+    if (kStore) emit32(out, a, lrow, 0, 1, 0, s0);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       w.add(normal_f32(s, c, zs, err));
       uint64_t u = s.next();
       if ((u >> 11) < M.jump_thr) jumps += fmaf(sigma_j, normal_f32(s, c, zs, err), mu_j);
       kf += 1.0f;
-      if (kStore) store32(a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value()) + jumps));
+      if (kStore) emit32(out, a, lrow, k, 1, 0, s0 * expf(fmaf(kf, drift, diffusion * w.value()) + jumps));
     }
     if (!kStore)
       pay[0] = payoff_f32(s0 * expf(fmaf(diffusion, w.value(), a.f32.m_kdrift) + jumps), a.f32.strike, a.payoff);
   };
   if constexpr (kStore) {
-    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads)
-      path(lrow, nullptr);
+    for_rows(a.rows, out, [&](uint64_t lrow) { path(lrow, nullptr); });
   } else {
     run_rows<1>(a, [&](uint64_t b, float* p) {
       const uint64_t lrow = b + (threadIdx.x & 31u);
@@ -765,13 +788,13 @@ FusedTune g_tune[kTuneSlots] = {{256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0}, 
 const void* fused_kernel(int slot, int ilp, int variant) {
   if (variant == 0) {  // the per-path loop kernels (one path per thread at a time)
     switch (slot) {
-      case 0: return (const void*)k_gbm_f32<false>;
-      case 1: return (const void*)k_heston_euler_f32<false>;
-      case 2: return (const void*)k_merton_f32<false>;
-      case 3: return (const void*)k_multi_gbm_f32<1, false>;
-      case 4: return (const void*)k_multi_gbm_f32<2, false>;
-      case 5: return (const void*)k_multi_gbm_f32<3, false>;
-      default: return (const void*)k_multi_gbm_f32<4, false>;
+      case 0: return (const void*)k_gbm_f32<kFused>;
+      case 1: return (const void*)k_heston_euler_f32<kFused>;
+      case 2: return (const void*)k_merton_f32<kFused>;
+      case 3: return (const void*)k_multi_gbm_f32<1, kFused>;
+      case 4: return (const void*)k_multi_gbm_f32<2, kFused>;
+      case 5: return (const void*)k_multi_gbm_f32<3, kFused>;
+      default: return (const void*)k_multi_gbm_f32<4, kFused>;
     }
   }
   if (variant == 2) {  // warp-uniform sampler feed (one path per thread)
@@ -797,15 +820,41 @@ const void* fused_kernel(int slot, int ilp, int variant) {
   }
 }
 
-template <bool kStore>
-void launch_multi32(const PathLaunch& L, dim3 g, dim3 b, cudaStream_t st) {
+template <int kMode>
+void launch_multi32(const PathLaunch& L, dim3 g, dim3 b, size_t sm, cudaStream_t st) {
   switch (L.multi.na) {
-    case 1: k_multi_gbm_f32<1, kStore><<<g, b, 0, st>>>(L); break;
-    case 2: k_multi_gbm_f32<2, kStore><<<g, b, 0, st>>>(L); break;
-    case 3: k_multi_gbm_f32<3, kStore><<<g, b, 0, st>>>(L); break;
-    case 4: k_multi_gbm_f32<4, kStore><<<g, b, 0, st>>>(L); break;
-    default: k_multi_gbm_f32<0, kStore><<<g, b, 0, st>>>(L); break;
+    case 1: k_multi_gbm_f32<1, kMode><<<g, b, sm, st>>>(L); break;
+    case 2: k_multi_gbm_f32<2, kMode><<<g, b, sm, st>>>(L); break;
+    case 3: k_multi_gbm_f32<3, kMode><<<g, b, sm, st>>>(L); break;
+    case 4: k_multi_gbm_f32<4, kMode><<<g, b, sm, st>>>(L); break;
+    default: k_multi_gbm_f32<0, kMode><<<g, b, sm, st>>>(L); break;
   }
+}
+
+// The untuned kernel of L's model in store mode kMode (occupancy query).
+template <int kMode>
+const void* model_kernel32(const PathLaunch& L) {
+  switch (L.model) {
+    case kGbm: return (const void*)k_gbm_f32<kMode>;
+    case kHeston: return (const void*)k_heston_euler_f32<kMode>;
+    case kMerton: return (const void*)k_merton_f32<kMode>;
+    default: return (const void*)k_multi_gbm_f32<3, kMode>;
+  }
+}
+
+template <int kMode>
+int launch_model32(const PathLaunch& L, dim3 G, dim3 B, size_t sm, cudaStream_t st) {
+  switch (L.model) {
+    case kGbm: k_gbm_f32<kMode><<<G, B, sm, st>>>(L); break;
+    case kHeston:
+      if (L.heston.scheme != 0) return -1;  // QE has no FP32 form
+      k_heston_euler_f32<kMode><<<G, B, sm, st>>>(L);
+      break;
+    case kMerton: k_merton_f32<kMode><<<G, B, sm, st>>>(L); break;
+    case kMultiGbm: launch_multi32<kMode>(L, G, B, sm, st); break;
+    default: return -1;
+  }
+  return 0;
 }
 
 }  // namespace
@@ -853,48 +902,35 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
     const bool queue = L.work != nullptr && !(variant == 1 && t.ilp == 2) && L.batch_rows >= 32 &&
                        L.batch_rows % 32 == 0;
     if (!queue) Lq.work = nullptr;
+    const uint64_t records = queue ? (L.rows + L.batch_rows - 1) / L.batch_rows : g;
+    if (L.max_records && records > L.max_records) return kRecordsExceeded;
     if (queue && cudaMemsetAsync(L.work, 0, sizeof(unsigned long long), st) != cudaSuccess) return -1;
     void* args[] = {(void*)&Lq};
     if (cudaLaunchKernel(fn, dim3((unsigned)g), dim3(t.block), args, 0, st) != cudaSuccess) return -1;
-    return queue ? (int)((L.rows + L.batch_rows - 1) / L.batch_rows) : (int)g;
+    return (int)records;
   }
   PathLaunch Ls = L;  // the untuned kernels below run static rows
   Ls.work = nullptr;
   const int b = 256;
+  const int mode = !store ? kFused : row_store_fits(L, sizeof(float)) ? kRows : kElems;
+  const size_t sm = mode == kRows ? RowStore<float>::bytes((uint32_t)b) : 0;
   // Persistent grid: exactly the blocks that are resident at once, so the
   // grid-stride loop gives every thread the same number of paths (+-1) in a
   // single wave instead of a partial second wave of blocks.
-  const void* fn = nullptr;
-  switch (L.model) {
-    case kGbm: fn = store ? (const void*)k_gbm_f32<true> : (const void*)k_gbm_f32<false>; break;
-    case kHeston: fn = store ? (const void*)k_heston_euler_f32<true> : (const void*)k_heston_euler_f32<false>; break;
-    case kMerton: fn = store ? (const void*)k_merton_f32<true> : (const void*)k_merton_f32<false>; break;
-    default: fn = store ? (const void*)k_multi_gbm_f32<3, true> : (const void*)k_multi_gbm_f32<3, false>; break;
-  }
+  const void* fn = mode == kRows ? model_kernel32<kRows>(L) : mode == kElems ? model_kernel32<kElems>(L)
+                                                                             : model_kernel32<kFused>(L);
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, b, 0) != cudaSuccess || per_sm < 1) per_sm = 2;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, b, sm) != cudaSuccess || per_sm < 1) per_sm = 2;
   uint64_t g = (L.rows + b - 1) / b;
   const uint64_t cap = (uint64_t)sms * per_sm;
   if (g > cap && !L.flat_grid) g = cap;
   if (g < 1) g = 1;
+  if (!store && L.max_records && g > L.max_records) return kRecordsExceeded;
   dim3 G((unsigned)g), B(b);
-  switch (L.model) {
-    case kGbm:
-      if (store) k_gbm_f32<true><<<G, B, 0, st>>>(Ls); else k_gbm_f32<false><<<G, B, 0, st>>>(Ls);
-      break;
-    case kHeston:
-      if (L.heston.scheme != 0) return -1;  // QE has no FP32 form
-      if (store) k_heston_euler_f32<true><<<G, B, 0, st>>>(Ls); else k_heston_euler_f32<false><<<G, B, 0, st>>>(Ls);
-      break;
-    case kMerton:
-      if (store) k_merton_f32<true><<<G, B, 0, st>>>(Ls); else k_merton_f32<false><<<G, B, 0, st>>>(Ls);
-      break;
-    case kMultiGbm:
-      if (store) launch_multi32<true>(Ls, G, B, st); else launch_multi32<false>(Ls, G, B, st);
-      break;
-    default:
-      return -1;
-  }
+  const int rc = mode == kRows ? launch_model32<kRows>(Ls, G, B, sm, st)
+                 : mode == kElems ? launch_model32<kElems>(Ls, G, B, 0, st)
+                                  : launch_model32<kFused>(Ls, G, B, 0, st);
+  if (rc < 0) return -1;
   return cudaPeekAtLastError() == cudaSuccess ? (int)g : -1;
 }
 

@@ -14,9 +14,14 @@
 #include "engine.h"
 #include "mc_device.cuh"
 #include "reduce.cuh"
+#include "row_store.cuh"
 
 namespace stocha {
 namespace {
+
+// Staging area of the row-major stores: RowStore<double>::bytes(blockDim.x)
+// bytes, passed at launch in the kRows mode.
+extern __shared__ __align__(16) unsigned char dyn_smem[];
 
 __device__ __forceinline__ double payoff_f64(double s, double k, int kind) {
   return kind == kCall ? fmax(s - k, 0.0) : fmax(k - s, 0.0);
@@ -57,15 +62,29 @@ __device__ __forceinline__ void store64(const PathLaunch& a, uint64_t lrow, uint
     a.out_f64[(lrow * (a.steps + 1) + step) * width + col] = v;
 }
 
-template <bool kStore>
+template <int kMode>
+using Out64 = PathOut<double, kMode>;
+
+template <int kMode>
+__device__ __forceinline__ void emit64(Out64<kMode>& out, const PathLaunch& a, uint64_t lrow, uint64_t step,
+                                       uint64_t width, uint64_t col, double v) {
+  if (kMode == kRows)
+    out.rs.put(v);
+  else if (kMode == kElems)
+    store64(a, lrow, step, width, col, v);
+}
+
+template <int kMode>
 __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   unsigned err = 0;
   double acc = 0.0, acc2 = 0.0;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  Out64<kMode> out;
+  out.init(dyn_smem);
+  for_rows(a.rows, out, [&](uint64_t lrow) {
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
@@ -73,7 +92,8 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
     // goes on the coefficient once per path (exact: IEEE products are odd)
     const double drift = a.gbm.drift, diffusion = neg ? -a.gbm.diffusion : a.gbm.diffusion;
     double x = a.gbm.s0;
-    if (kStore) store64(a, lrow, 0, 1, 0, x);
+    if (kMode == kRows) out.begin(a.out_f64 + lrow * (a.steps + 1));
+    if (kStore) emit64(out, a, lrow, 0, 1, 0, x);
     // Two steps at a time: both draws, then both exponentials (independent
     // chains the compiler interleaves), then the two dependent products.  At
     // small path counts a warp's step is latency-bound on the exponential's
@@ -86,27 +106,28 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
       const double y0 = exp_y(fma(diffusion, z0, drift), zs);
       const double y1 = exp_y(fma(diffusion, z1, drift), zs);
       x *= y0;
-      if (kStore) store64(a, lrow, k, 1, 0, x);
+      if (kStore) emit64(out, a, lrow, k, 1, 0, x);
       x *= y1;
-      if (kStore) store64(a, lrow, k + 1, 1, 0, x);
+      if (kStore) emit64(out, a, lrow, k + 1, 1, 0, x);
     }
     if (k <= a.steps) {
       const double z = normal_f64(s, c, zs, err);
       x = mul_exp(x, fma(diffusion, z, drift), zs);
-      if (kStore) store64(a, lrow, k, 1, 0, x);
+      if (kStore) emit64(out, a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
       double p = launch_payoff(a, x);
       acc += p;
       acc2 += p * p;
     }
-  }
+  });
   if (!kStore) block_sum2_store(acc, acc2, a.partials + 2 * blockIdx.x);
   if (err) atomicOr(a.err, err);
 }
 
-template <int NA, bool kStore>
+template <int NA, int kMode>
 __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -114,18 +135,20 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
   unsigned err = 0;
   double acc[NA > 0 ? NA : kMaxAssets], acc2[NA > 0 ? NA : kMaxAssets];
   for (int i = 0; i < na; ++i) acc[i] = acc2[i] = 0.0;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  Out64<kMode> out;
+  out.init(dyn_smem);
+  for_rows(a.rows, out, [&](uint64_t lrow) {
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
     double sv[NA > 0 ? NA : kMaxAssets], z[NA > 0 ? NA : kMaxAssets], dif[NA > 0 ? NA : kMaxAssets];
+    if (kMode == kRows) out.begin(a.out_f64 + lrow * (a.steps + 1) * na);
 #pragma unroll
     for (int i = 0; i < na; ++i) {
       sv[i] = a.multi.s0[i];
       // antithetic sign on the coefficient: L(-z) = -(L z) exactly
       dif[i] = neg ? -a.multi.diffusion[i] : a.multi.diffusion[i];
-      if (kStore) store64(a, lrow, 0, na, i, sv[i]);
+      if (kStore) emit64(out, a, lrow, 0, na, i, sv[i]);
     }
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
@@ -138,7 +161,7 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
 #pragma unroll
         for (int m = 1; m <= i; ++m) eps = fma(a.multi.L[i * kMaxAssets + m], z[m], eps);
         sv[i] = mul_exp(sv[i], fma(dif[i], eps, a.multi.drift[i]), zs);
-        if (kStore) store64(a, lrow, k, na, i, sv[i]);
+        if (kStore) emit64(out, a, lrow, k, na, i, sv[i]);
       }
     }
     if (!kStore) {
@@ -149,27 +172,30 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
         acc2[i] += p * p;
       }
     }
-  }
+  });
   if (!kStore) {
     for (int i = 0; i < na; ++i) block_sum2_store(acc[i], acc2[i], a.partials + (2 * (uint64_t)blockIdx.x) * na + 2 * i);
   }
   if (err) atomicOr(a.err, err);
 }
 
-template <bool kStore>
+template <int kMode>
 __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const HestonK& h = a.heston;
   unsigned err = 0;
   double acc = 0.0, acc2 = 0.0;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  Out64<kMode> out;
+  out.init(dyn_smem);
+  for_rows(a.rows, out, [&](uint64_t lrow) {
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     double x = h.s0, v = h.v0;
-    if (kStore) store64(a, lrow, 0, 1, 0, x);
+    if (kMode == kRows) out.begin(a.out_f64 + lrow * (a.steps + 1));
+    if (kStore) emit64(out, a, lrow, 0, 1, 0, x);
     if (h.scheme == 0) {
       const double mu_dt = h.mu * h.dt, nhalf_dt = -0.5 * h.dt;
 #pragma unroll 1
@@ -184,7 +210,7 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
         // (mu - v+/2) dt + sqrt(v+ dt) dW1 only feeds x, so it is fused
         v += h.kappa * (h.theta - v_plus) * h.dt + h.xi * sqrt_v * h.sqrt_dt * dw2;
         x = mul_exp(x, fma(sqrt_v * h.sqrt_dt, dw1, fma(nhalf_dt, v_plus, mu_dt)), zs);
-        if (kStore) store64(a, lrow, k, 1, 0, x);
+        if (kStore) emit64(out, a, lrow, k, 1, 0, x);
       }
     } else {
 #pragma unroll 1
@@ -214,7 +240,7 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
         double log_s = log(x) + h.k0_s + h.k1_s * v_plus + h.k2_s * v_next + sqrt(var_term) * z1;
         x = exp(fmin(fmax(log_s, -500.0), 500.0));
         v = v_next;
-        if (kStore) store64(a, lrow, k, 1, 0, x);
+        if (kStore) emit64(out, a, lrow, k, 1, 0, x);
       }
     }
     if (!kStore) {
@@ -222,25 +248,28 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
       acc += p;
       acc2 += p * p;
     }
-  }
+  });
   if (!kStore) block_sum2_store(acc, acc2, a.partials + 2 * blockIdx.x);
   if (err) atomicOr(a.err, err);
 }
 
-template <bool kStore>
+template <int kMode>
 __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const MertonK& M = a.merton;
   unsigned err = 0;
   double acc = 0.0, acc2 = 0.0;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  Out64<kMode> out;
+  out.init(dyn_smem);
+  for_rows(a.rows, out, [&](uint64_t lrow) {
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     double x = M.s0;
-    if (kStore) store64(a, lrow, 0, 1, 0, x);
+    if (kMode == kRows) out.begin(a.out_f64 + lrow * (a.steps + 1));
+    if (kStore) emit64(out, a, lrow, 0, 1, 0, x);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       const double z = normal_f64(s, c, zs, err);
@@ -251,39 +280,42 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
         ret += fma(M.sigma_j, z_j, M.mu_j);
       }
       x = mul_exp<false>(x, ret, zs);  // issue-bound: the early-exit form
-      if (kStore) store64(a, lrow, k, 1, 0, x);
+      if (kStore) emit64(out, a, lrow, k, 1, 0, x);
     }
     if (!kStore) {
       double p = launch_payoff(a, x);
       acc += p;
       acc2 += p * p;
     }
-  }
+  });
   if (!kStore) block_sum2_store(acc, acc2, a.partials + 2 * blockIdx.x);
   if (err) atomicOr(a.err, err);
 }
 
 // Hull-White one-factor short rate by its exact Gaussian transition
 // (hull_white.rs:26-57): r <- r * e + (theta/a)(1 - e) + vol * z; paths only.
+template <int kMode>
 __global__ void __launch_bounds__(128) k_hull_white_f64(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const HullWhiteK& H = a.hw;
   unsigned err = 0;
-  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t lrow = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; lrow < a.rows; lrow += nthreads) {
+  Out64<kMode> out;
+  out.init(dyn_smem);
+  for_rows(a.rows, out, [&](uint64_t lrow) {
     const uint64_t row = a.row_begin + lrow;
     PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
     double x = H.r0;
-    store64(a, lrow, 0, 1, 0, x);
+    if (kMode == kRows) out.begin(a.out_f64 + lrow * (a.steps + 1));
+    emit64(out, a, lrow, 0, 1, 0, x);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
       const double z = normal_f64(s, c, zs, err);
       x = x * H.e + H.mean_reversion + H.vol * z;
-      store64(a, lrow, k, 1, 0, x);
+      emit64(out, a, lrow, k, 1, 0, x);
     }
-  }
+  });
   if (err) atomicOr(a.err, err);
 }
 
@@ -320,14 +352,31 @@ __global__ void __launch_bounds__(256) k_reduce_partials(const double* __restric
   if (threadIdx.x == 0) out[v] = sh[0];
 }
 
-template <bool kStore>
-int launch_multi(const PathLaunch& L, dim3 g, dim3 b, cudaStream_t st) {
+template <int kMode>
+int launch_multi(const PathLaunch& L, dim3 g, dim3 b, size_t sm, cudaStream_t st) {
   switch (L.multi.na) {
-    case 1: k_multi_gbm_f64<1, kStore><<<g, b, 0, st>>>(L); break;
-    case 2: k_multi_gbm_f64<2, kStore><<<g, b, 0, st>>>(L); break;
-    case 3: k_multi_gbm_f64<3, kStore><<<g, b, 0, st>>>(L); break;
-    case 4: k_multi_gbm_f64<4, kStore><<<g, b, 0, st>>>(L); break;
-    default: k_multi_gbm_f64<0, kStore><<<g, b, 0, st>>>(L); break;
+    case 1: k_multi_gbm_f64<1, kMode><<<g, b, sm, st>>>(L); break;
+    case 2: k_multi_gbm_f64<2, kMode><<<g, b, sm, st>>>(L); break;
+    case 3: k_multi_gbm_f64<3, kMode><<<g, b, sm, st>>>(L); break;
+    case 4: k_multi_gbm_f64<4, kMode><<<g, b, sm, st>>>(L); break;
+    default: k_multi_gbm_f64<0, kMode><<<g, b, sm, st>>>(L); break;
+  }
+  return 0;
+}
+
+template <int kMode>
+int launch_model(const PathLaunch& L, dim3 G, dim3 B, size_t sm, cudaStream_t st) {
+  switch (L.model) {
+    case kGbm: k_gbm_f64<kMode><<<G, B, sm, st>>>(L); break;
+    case kHeston: k_heston_f64<kMode><<<G, B, sm, st>>>(L); break;
+    case kMerton: k_merton_f64<kMode><<<G, B, sm, st>>>(L); break;
+    case kMultiGbm: launch_multi<kMode>(L, G, B, sm, st); break;
+    case kHullWhite:
+      if (kMode == kFused) return -1;  // rate paths have no in-kernel payoff
+      k_hull_white_f64<kMode == kFused ? kElems : kMode><<<G, B, sm, st>>>(L);
+      break;
+    default:
+      return -1;
   }
   return 0;
 }
@@ -353,27 +402,14 @@ int launch_paths_f64(const PathLaunch& L, cudaStream_t st) {
   int g, b;
   pick_grid(L.rows, &g, &b);
   const bool store = L.out_f64 != nullptr;
+  if (!store && L.max_records && (uint64_t)g > L.max_records) return kRecordsExceeded;
+  const int mode = !store ? kFused : row_store_fits(L, sizeof(double)) ? kRows : kElems;
+  const size_t sm = mode == kRows ? RowStore<double>::bytes((uint32_t)b) : 0;
   dim3 G(g), B(b);
-  switch (L.model) {
-    case kGbm:
-      if (store) k_gbm_f64<true><<<G, B, 0, st>>>(L); else k_gbm_f64<false><<<G, B, 0, st>>>(L);
-      break;
-    case kHeston:
-      if (store) k_heston_f64<true><<<G, B, 0, st>>>(L); else k_heston_f64<false><<<G, B, 0, st>>>(L);
-      break;
-    case kMerton:
-      if (store) k_merton_f64<true><<<G, B, 0, st>>>(L); else k_merton_f64<false><<<G, B, 0, st>>>(L);
-      break;
-    case kMultiGbm:
-      if (store) launch_multi<true>(L, G, B, st); else launch_multi<false>(L, G, B, st);
-      break;
-    case kHullWhite:
-      if (!store) return -1;  // rate paths have no in-kernel payoff
-      k_hull_white_f64<<<G, B, 0, st>>>(L);
-      break;
-    default:
-      return -1;
-  }
+  const int rc = mode == kRows ? launch_model<kRows>(L, G, B, sm, st)
+                 : mode == kElems ? launch_model<kElems>(L, G, B, 0, st)
+                                  : launch_model<kFused>(L, G, B, 0, st);
+  if (rc < 0) return -1;
   return cudaPeekAtLastError() == cudaSuccess ? g : -1;
 }
 

@@ -1,0 +1,114 @@
+"""Row-major path output through the staged sector writer (row_store.cuh).
+
+The materialised kernels write each row in whole 32-byte sectors: a lane
+stages its values in shared memory and stores a sector when it is complete;
+the sector two rows share is merged across neighbouring lanes at the end of
+the row; sectors whose neighbour row is not in the warp (a launch's first or
+last rows, or a launch that does not start on a sector boundary) are written
+element by element.  These tests cover the layouts where that logic has
+cases: row lengths around the two-sector minimum, partial warps, every
+phase of a row within its first sector, multi-asset rows, and chunked
+launches whose base is not sector-aligned.
+
+Bars: FP64 paths equal the oracle within PATH_RTOL (the FP64 parity bar);
+FP32 rows are all written (no NaN sentinel left) and within F32_RTOL of the
+FP64 paths of the same draws.
+"""
+import ctypes
+import gc
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+PATH_RTOL = 1e-12
+# FP32 materialised paths: log-space compensated sums and one expf per value;
+# measured ~1e-6 relative at 252 steps
+F32_RTOL = 2e-5
+
+
+def _rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300))) if a.size else 0.0
+
+
+@pytest.mark.parametrize("steps", [6, 7, 8, 9, 10, 11, 15, 16, 17])
+@pytest.mark.parametrize("n", [1, 2, 31, 32, 33, 65, 257])
+def test_gbm_row_lengths_and_partial_warps(stocha, oracle, steps, n):
+    got = stocha.gbm(100.0, 0.05, 0.2, 1.0, steps, n, seed=3)
+    want = oracle.gbm(100.0, 0.05, 0.2, 1.0, steps, n, seed=3)
+    assert got.shape == (n, steps + 1)
+    assert _rel(got, want) <= PATH_RTOL
+
+
+@pytest.mark.parametrize("na,steps", [(2, 3), (2, 4), (3, 2), (3, 3), (3, 7), (4, 1), (5, 1), (5, 2), (7, 5)])
+def test_multi_gbm_row_layouts(stocha, oracle, na, steps):
+    rng = np.random.default_rng(10 * na + steps)
+    a = rng.normal(size=(na, na))
+    cov = a @ a.T + na * np.eye(na)
+    d = np.sqrt(np.diag(cov))
+    corr = cov / np.outer(d, d)
+    args = (list(rng.uniform(50, 200, na)), list(rng.uniform(0.0, 0.1, na)), list(rng.uniform(0.1, 0.4, na)), corr,
+            1.0, steps, 97)
+    got = stocha.multi_gbm(*args, seed=4)
+    want = oracle.multi_gbm(*args, seed=4)
+    assert got.shape == (97, steps + 1, na)
+    assert _rel(got, want) <= PATH_RTOL
+
+
+def test_chunks_not_sector_aligned(stocha, oracle):
+    """2^21 + 8 rows of 9 doubles into a cached host buffer: the overlap path
+    computes 8 chunks of 262145 rows, so chunk k starts k * 262145 * 9
+    elements into the array, off the 4-element sector grid for odd k.  The
+    result must equal the one-launch result (first call, fresh memory) and
+    the oracle around every chunk boundary."""
+    n, steps = (1 << 21) + 8, 8
+    kw = dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=steps, n_paths=n, seed=21)
+    a = stocha.gbm(**kw)
+    assert a.nbytes >= 64 << 20
+    first = a.copy()
+    del a
+    gc.collect()
+    b = stocha.gbm(**kw)  # the cached buffer: chunked launches
+    np.testing.assert_array_equal(b, first)
+    per = (n + 7) // 8
+    k = 7 * per + 40
+    want = oracle.gbm(100.0, 0.05, 0.2, 1.0, steps, k, seed=21, threads=8)
+    for c in range(1, 8):
+        lo, hi = c * per - 40, c * per + 40
+        assert _rel(b[lo:hi], want[lo:hi]) <= PATH_RTOL, c
+
+
+def _paths_device(stocha, torch, model, params, steps, n, precision, seed=42):
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    m = stocha.model_struct(model, params, steps=steps, n_paths=n)
+    width = m.n_assets if model == "multi_gbm" else 1
+    shape = (n, steps + 1, width) if model == "multi_gbm" else (n, steps + 1)
+    dt = torch.float32 if precision == "fp32" else torch.float64
+    out = torch.full(shape, float("nan"), dtype=dt, device="cuda")
+    prec = _lib.FP32 if precision == "fp32" else _lib.FP64
+    _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), seed, prec, ctypes.c_void_p(out.data_ptr())))
+    _lib.check(lib.stocha_ctx_sync(None))
+    return out.cpu().numpy()
+
+
+HESTON = dict(s0=100.0, v0=0.04, mu=0.05, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7, t=1.0)
+MERTON = dict(s0=100.0, mu=0.05, sigma=0.2, lambda_=1.0, mu_j=-0.05, sigma_j=0.1, t=1.0)
+MULTI = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.15],
+             corr=np.array([[1, .6, .3], [.6, 1, .5], [.3, .5, 1]], float), t=1.0)
+GBM = dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0)
+
+
+@pytest.mark.parametrize("model,params", [("gbm", GBM), ("heston", HESTON), ("merton", MERTON),
+                                          ("multi_gbm", MULTI)])
+@pytest.mark.parametrize("steps,n", [(15, 1), (16, 33), (17, 250), (52, 4099), (252, 20_000)])
+def test_fp32_rows_written_and_close_to_fp64(stocha, model, params, steps, n):
+    torch = pytest.importorskip("torch")
+    p32 = _paths_device(stocha, torch, model, params, steps, n, "fp32")
+    assert not np.isnan(p32).any()  # every element written exactly where it belongs
+    p64 = _paths_device(stocha, torch, model, params, steps, n, "fp64")
+    assert _rel(p32, p64) <= F32_RTOL
