@@ -183,10 +183,15 @@ int stocha_price_device(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, i
 /* Fused pricing without any device allocation (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc: a host application
  * that owns all device memory, or a request path that must never reach the
- * allocator.  Same kernels and output as stocha_price_device (out_dev: 2 *
- * n_assets doubles of raw payoff sums, caller-owned device memory), on the
- * caller's cudaStream_t; scratch, tables and status live in static device
- * arrays of the library (1 MiB of scratch: at most 4 assets).  Synchronous:
+ * allocator.  Same kernels as stocha_price_device (out_dev: 2 * n_assets
+ * doubles of raw payoff sums, caller-owned device memory), on the caller's
+ * cudaStream_t; scratch, tables and status live in static device arrays of
+ * the library (1 MiB of scratch: at most 4 assets, 16384 partial records).
+ * The sums are bit-equal to stocha_price_device's for FP64, and for FP32 up
+ * to 524,288 rows; above that the FP32 work-queue batches grow past 32 rows
+ * to fit the records, the sums are grouped differently and agree to FP32
+ * rounding.  A launch that would need more records is refused (value error)
+ * before anything runs.  Synchronous:
  * waits for `stream` and reports device-check failures.  The first call on a
  * device sets up its arrays (make it before any stream capture); calls that
  * overlap on the GPU share the arrays and race. */

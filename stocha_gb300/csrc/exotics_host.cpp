@@ -593,6 +593,9 @@ int stocha_asian_price(stocha_ctx* ctx, double s, double k, double r, double sig
     return set_error(STOCHA_ERR_VALUE, "Unknown method: '" + m + "'. Supported: 'auto', 'analytical', 'mc'");
   }
   if (p.n_steps == 0) return set_error(STOCHA_ERR_VALUE, "n_steps must be positive");
+  // the device's Asian log sum weights each step exponent by an integer built
+  // as an exact double, which holds below 2^53 steps
+  if (p.n_steps >= (1ull << 53)) return set_error(STOCHA_ERR_VALUE, "n_steps must be below 2^53");
   if ((rc = with_ctx(&ctx))) return rc;
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   return asian_mc(ctx, p, n_paths, seed, price);

@@ -12,8 +12,9 @@
 // the caller passes the output buffer and the stream.
 //
 // Limits.  The scratch array holds kNoAllocMaxBlocks partial records of up to
-// kNoAllocMaxAssets assets (1 MiB).  Calls for more assets, or on a GPU whose
-// launch grid would exceed the record count, are rejected with an error.
+// kNoAllocMaxAssets assets (1 MiB).  Calls for more assets, or whose launch
+// would write more records than that, are rejected with an error before
+// anything is launched.
 // Every GPU that loads the library keeps these arrays until the process exits.
 //
 // Set-up.  The first call on a device (with that device current) takes the
@@ -96,11 +97,8 @@ extern "C" int stocha_price_noalloc(const stocha_model* m, uint64_t seed, int32_
     return set_error(STOCHA_ERR_VALUE, "stocha_price_noalloc prices at most " + std::to_string(kNoAllocMaxAssets) +
                                            " assets (its static scratch holds " + std::to_string(kNoAllocMaxBlocks) +
                                            " partial records of " + std::to_string(kNoAllocMaxAssets) + " assets)");
-  int dev = 0, sms = 0;
+  int dev = 0;
   STOCHA_CUDA(cudaGetDevice(&dev));
-  STOCHA_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  if ((uint64_t)sms * 64 > (uint64_t)kNoAllocMaxBlocks)  // largest grid the path launchers pick
-    return set_error(STOCHA_ERR_VALUE, "stocha_price_noalloc: this GPU's launch grid exceeds the static scratch");
   DeviceArrays* d = nullptr;
   if ((rc = setup(dev, &d))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
@@ -117,20 +115,28 @@ extern "C" int stocha_price_noalloc(const stocha_model* m, uint64_t seed, int32_
   }
   L.strike = strike;
   L.payoff = payoff;
+  // the launchers compute their record count first and launch nothing when it
+  // exceeds the static scratch, so no launch can write past the array
+  L.max_records = kNoAllocMaxBlocks;
   fill_f32_constants(&L);
   STOCHA_CUDA(cudaMemsetAsync(d->status, 0, sizeof(unsigned), st));
   if (L.rows == 0) {
     STOCHA_CUDA(cudaMemsetAsync(sums_dev, 0, 2 * na * sizeof(double), st));
   } else {
     const int nb = precision == STOCHA_FP32 ? launch_paths_f32(L, st) : launch_paths_f64(L, st);
+    if (nb == kRecordsExceeded)
+      return set_error(STOCHA_ERR_VALUE, "stocha_price_noalloc: the launch would need more than " +
+                                             std::to_string(kNoAllocMaxBlocks) +
+                                             " partial records (the static scratch's size)");
     if (nb < 0) return cuda_error(cudaGetLastError(), "pricing kernel launch");
-    if (nb > kNoAllocMaxBlocks) return set_error(STOCHA_ERR_DEVICE, "launch grid exceeded the static scratch");
     launch_reduce_partials(d->scratch, nb, 2 * na, sums_dev, st);
   }
   STOCHA_CUDA(cudaGetLastError());
-  STOCHA_CUDA(cudaStreamSynchronize(st));
+  // the status word comes back on the caller's stream: no wait on the legacy
+  // default stream (and so on the application's other blocking streams)
   unsigned status = 0;
-  STOCHA_CUDA(cudaMemcpy(&status, d->status, sizeof status, cudaMemcpyDeviceToHost));
+  STOCHA_CUDA(cudaMemcpyAsync(&status, d->status, sizeof status, cudaMemcpyDeviceToHost, st));
+  STOCHA_CUDA(cudaStreamSynchronize(st));
   if (status) return set_error(STOCHA_ERR_DEVICE, "device check failed (sampler iteration cap)");
   return STOCHA_OK;
 }

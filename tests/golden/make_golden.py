@@ -66,8 +66,9 @@ def main():
     with open(os.path.join(HERE, "pcg64dxsm_numpy.json"), "w") as f:
         json.dump({"generator": "numpy.random.PCG64DXSM", "numpy": np.__version__, "cases": pcg_cases()}, f,
                   indent=1)
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if os.path.exists(os.path.join(ref, "src/dist/ziggurat_tables.rs")):
+    # the reference checkout: first argument, else STOCHA_REFERENCE_ROOT
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("STOCHA_REFERENCE_ROOT", "")
+    if ref and os.path.exists(os.path.join(ref, "src/dist/ziggurat_tables.rs")):
         with open(os.path.join(HERE, "ziggurat_ref.json"), "w") as f:
             json.dump(table_hash(ref), f, indent=1)
 

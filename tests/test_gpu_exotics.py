@@ -4,8 +4,9 @@ against the oracle's restatement (same streams, same GBM step).
 Bars: FP64 prices within MC_RTOL of the oracle (summation order and the
 kernels' exponential: paths agree to ~1e-14 relative; a barrier decision
 could flip only for a path within that of the barrier); the Asian
-geometric average is carried in log space (ln s_k as a running sum of the
-step exponents), within ASIAN_RTOL.  The reference's own MC expectations
+geometric average's log sum is n ln s0 + sum_i (n - i + 1) x_i over the step
+exponents x_i, one weighted FMA a step (the oracle keeps the reference's
+running log and its running sum), within ASIAN_RTOL.  The reference's own MC expectations
 (agreement with the closed forms, reproducibility) are restated.
 """
 import math

@@ -16,6 +16,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 SUM_RTOL = 1e-12  # same kernels and reduction order: the tolerance of the FP64 price tests
+# Above 524,288 FP32 rows the allocation-free form takes 64-row work-queue
+# batches (its 16384 records would not hold 32-row ones), so the FP32 payoff
+# sums are grouped differently from stocha_price_device's: they agree to FP32
+# rounding of the per-batch sums, far inside the 1e-4 FP32 price bar.
+GROUPED_RTOL = 1e-6
 
 HESTON = dict(s0=100.0, v0=0.04, mu=0.05, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7, t=1.0)
 MULTI = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.15],
@@ -24,6 +29,7 @@ MULTI = dict(s0=[100.0, 50.0, 200.0], mu=[0.05, 0.08, 0.03], sigma=[0.2, 0.3, 0.
 
 @pytest.mark.parametrize("model,params,precision,n", [("heston", HESTON, "fp64", 20_000),
                                                        ("heston", HESTON, "fp32", 300_000),
+                                                       ("heston", HESTON, "fp32", 600_000),
                                                        ("multi_gbm", MULTI, "fp64", 10_000),
                                                        ("gbm", dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0), "fp32", 1)])
 def test_noalloc_matches_price_device(stocha, model, params, precision, n):
@@ -46,7 +52,8 @@ def test_noalloc_matches_price_device(stocha, model, params, precision, n):
         _lib.check(lib.stocha_price_noalloc(ctypes.byref(m), 42, prec, _lib.PAYOFF_CALL, 100.0,
                                             ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(stream.cuda_stream)))
         got = out.cpu().numpy()
-        assert np.all(np.abs(got - want) <= SUM_RTOL * np.abs(want)), (got, want)
+        rtol = GROUPED_RTOL if precision == "fp32" and n > 524_288 else SUM_RTOL
+        assert np.all(np.abs(got - want) <= rtol * np.abs(want)), (got, want)
 
 
 def test_noalloc_rejects_beyond_its_scratch(stocha):
