@@ -1,39 +1,33 @@
-"""Benchmark: path-steps/s, FP32 fused vs FP64 plain, on the correlated and
-stochastic-volatility workload (1e6 paths x 252 steps of each of: 3-asset
-multi-GBM, Heston (Euler), Merton; seed 42; European call at K=100).
+"""Benchmark: path-steps/s of the correlated and stochastic-volatility
+workload (1e6 paths x 252 steps of each of: 3-asset multi-GBM, Heston
+(Euler), Merton; seed 42), FP64 plain and FP32 fused.
 
 One "step" = one pass of all three models.  Path-steps per step = 3 * 2.52e8
 (one path-step = one time step of one path, all assets for multi-GBM).
 
-  value   FP32 fused pricing, device-resident (parameters only, no inputs),
-          timed with CUDA events on the launching stream.
-  e2e     the same through the public API stocha_gb300.price_european
-          (host call: parameters in, (price, se) out, copies included).
-  autotune  the fused FP32 kernels' launch shapes (threads per block, paths
-          per thread in lockstep, grid waves), timed on this workload before
-          the timed region; the chosen shape and its gain over the default.
-  fp64_plain   FP64 materialised paths (reference arithmetic) of the same
-          workload into device memory (10.1 GB per step) and, end to end,
-          through stocha_gb300.multi_gbm/heston/merton_jump_diffusion into
-          host NumPy arrays.
-  roofline  dominant kernel = FP32 fused; bound = the PCG64DXSM generator
-          (integer pipes): achieved draws/s vs the measured draw rate of the
-          generator alone (stocha_measure_peak kind 3).
+  value     FP64 plain (the reference's method and precision): the three
+            models' FP64 paths materialised into device memory (10.1 GB per
+            step), timed with CUDA events on the launching stream.
+  e2e       the same through the public API stocha_gb300.multi_gbm / heston /
+            merton_jump_diffusion into host NumPy arrays (copies included).
+  roofline  the dominant FP64 plain kernel against the FP64 pipe (measured
+            DFMA rate), with its HBM write rate beside it.
+  fp32_fused         FP32 paths reduced in-kernel to a European call (K=100):
+            device rate, e2e through price_european, autotuned launch shapes,
+            the speed-up over FP64 plain, and the generator-bound roofline.
+  fp64_fused, fp32_materialised   the configuration's other two cells.
   cpu_baseline  the C++ oracle (restatement of the reference's Rayon
-          algorithm) on the host cores, bounded sample.
+            algorithm) on the host cores, bounded sample.
   config5_serving  20 000 pricing / Greeks / LSMC requests, Poisson arrivals
-          at 2000/s, through stocha_gb300.Server (40 GB budget): p50/p99
-          latency overall and for requests of <= 1e5 paths, requests/s, and
-          the per-request error of a sample against the FP64 plain form.
-  exotics_mc, rates_copulas_risk, api_rows  barrier / Asian / lookback
-          Monte Carlo, Hull-White paths, Gaussian and Student-t copulas,
-          VaR/CVaR, the RNG class, greeks_fd and greeks_pathwise through the
-          public API (host arrays), each beside the oracle on a bounded
-          sample.
+            at 2000/s, through stocha_gb300.Server (40 GB budget): p50/p99
+            latency overall and for requests of <= 1e5 paths, requests/s, and
+            the per-request error against the FP64 plain form.
+  config1_gbm_fp64, config3_lsmc, config4_greeks_batch, exotics_mc,
+  rates_copulas_risk, api_rows   the other configurations and rows through
+            the public API, each beside the oracle on a bounded sample.
 
 --impl reference runs the C++ oracle (the reference itself is Rust and cannot
-be built here) on all host cores for the same workload, each step a sample of
-1e5 paths per model.
+be built here) on all host cores over the identical headline workload.
 """
 from __future__ import annotations
 
@@ -138,7 +132,8 @@ class ClockSampler:
 
 def cpu_baseline(threads: int, sample_paths: int):
     """Oracle (C++ restatement of the reference's algorithm) on host cores:
-    FP64 materialised paths + payoff of the three models, sample_paths each."""
+    FP64 paths of the three models gathered into host arrays, sample_paths
+    each."""
     import numpy as np
 
     from oracle import oracle as O
@@ -148,15 +143,13 @@ def cpu_baseline(threads: int, sample_paths: int):
     t0 = time.perf_counter()
     p = O.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, sample_paths, seed=SEED,
                     threads=threads, gather=True)
-    _ = np.maximum(p[:, -1, :] - STRIKE, 0).mean(axis=0)
     del p
     p = O.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")], STEPS, sample_paths,
                  seed=SEED, threads=threads, gather=True)
-    _ = np.maximum(p[:, -1] - STRIKE, 0).mean()
     del p
     p = O.merton(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j", "sigma_j", "t")], STEPS,
                  sample_paths, seed=SEED, threads=threads, gather=True)
-    _ = np.maximum(p[:, -1] - STRIKE, 0).mean()
+    del p
     dt = time.perf_counter() - t0
     return 3 * sample_paths * STEPS / dt
 
@@ -518,29 +511,91 @@ def replica_seed(rank: int) -> int:
     return SEED + rank
 
 
+# The headline configuration, written identically into both arms' lines
+def headline_config(seed=SEED):
+    return {"workload": "multi_gbm(3 assets, corr [[1,.6,.3],[.6,1,.5],[.3,.5,1]]) + heston(euler) + "
+                        "merton(lambda=1, mu_j=-0.05, sigma_j=0.1); 252 steps; 1e6 paths each; seed 42; "
+                        "FP64 paths materialised (n_paths, steps+1[, n_assets]), the reference's method",
+            "paths_per_model": N_PATHS, "steps": STEPS, "seed": seed, "precision": "fp64", "mode": "materialised",
+            "l2": "no input data (parameters only); the 10.1 GB of FP64 paths written per step exceed L2"}
+
+
+# FP64 pipe operations per path-step that each FP64 plain kernel issues
+# (DMUL, DADD, DFMA counted once), read from the kernels: the exponential,
+# the sqrt, the conversions and (multi-GBM, Heston) the normals' products run
+# on the integer pipes.
+#   multi-GBM(3): Cholesky rows 3 DMUL + 3 DFMA; per asset exponent DFMA + product DMUL
+#   Heston Euler: correlated normal 3; variance recursion 8; log increment 3; product 1
+#   Merton: normal product, exponent DFMA, price product (+3 on the ~0.4 % jump steps)
+FP64_OPS_PER_PATH_STEP = {"multi_gbm": 12.0, "heston": 15.0, "merton": 3.0 + 3.0 / 252}
+
+
+def oracle_headline_step(cores):
+    """One step of the headline workload on the host cores by the oracle (the
+    C++ restatement of the reference's Rayon algorithm): the three models'
+    FP64 paths, each gathered serially into a new array as gbm.rs:99-105
+    does.  Returns the seconds taken."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    corr = np.array(CORR3)
+    t0 = time.perf_counter()
+    p = O.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, N_PATHS, seed=SEED, threads=cores,
+                    gather=True)
+    del p
+    p = O.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")], STEPS, N_PATHS,
+                 seed=SEED, threads=cores, gather=True)
+    del p
+    p = O.merton(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j", "sigma_j", "t")], STEPS, N_PATHS,
+                 seed=SEED, threads=cores, gather=True)
+    del p
+    return time.perf_counter() - t0
+
+
 def run_reference(args, rank, world):
+    """The reference's own CPU algorithm on the headline configuration.  The
+    reference is Rust and cannot be built here, so this is the oracle, its
+    C++ restatement, on all host cores, over the same 3 x 1e6 x 252 FP64
+    paths as the GPU arm's headline (same config, same seed)."""
     if rank != 0:
         return
+    from oracle import oracle as O
+
+    O.build()
     cores = host_cores()
-    sample = 100_000
     for _ in range(args.warmup):
-        cpu_baseline(cores, sample)
-    vals = [cpu_baseline(cores, sample) for _ in range(args.steps)]
-    total_time = sum(3 * sample * STEPS / v for v in vals)
-    value = 3 * sample * STEPS * len(vals) / total_time
+        oracle_headline_step(cores)
+    times = [oracle_headline_step(cores) for _ in range(args.steps)]
+    total = sum(times)
+    path_steps = 3 * N_PATHS * STEPS
+    value = path_steps * len(times) / total
     line = {
         "impl": "reference", "metric": "path-steps/s", "value": value, "unit": "path-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * total_time / len(vals), "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference parameters)",
-        "config": {"workload": "multi_gbm(3 assets)+heston(euler)+merton, 252 steps, european call K=100",
-                   "paths_per_model_per_step": sample, "full_paths_per_model": N_PATHS},
+        "config": headline_config(),
         "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{sample} paths x {STEPS} steps per model, FP64 materialised + payoff"},
+                         "sample": f"the full workload: 3 models x {N_PATHS} paths x {STEPS} steps, FP64 paths "
+                                   "gathered into host arrays"},
         "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "C++ restatement of stocha's Rayon algorithm (the Rust reference cannot be built here)",
     }
     print(json.dumps(line), flush=True)
+
+
+def _events(stream, fn, reps):
+    """Average ms of fn() over reps, CUDA events on `stream`."""
+    import torch
+
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    b.synchronize()
+    return a.elapsed_time(b) / reps
 
 
 def run_ours(args, rank, world):
@@ -563,20 +618,7 @@ def run_ours(args, rank, world):
     _lib.check(lib.stocha_ctx_create(dev, ctypes.byref(ctx)))
     stream = torch.cuda.Stream()
     _lib.check(lib.stocha_ctx_set_stream(ctx, ctypes.c_void_p(stream.cuda_stream)))
-    seed = replica_seed(rank)  # weak scaling: each rank prices its own independent 1e6 paths per model
-
-    models = [(name, stocha.model_struct(name, p, STEPS, N_PATHS)) for name, p in WORKLOAD]
-    # launch shapes of the fused FP32 kernels, tuned on this workload before any timing
-    tuning = {}
-    if not args.no_tune:
-        for name, p in WORKLOAD:
-            tuning[name] = stocha.autotune(name, p, steps=STEPS, n_paths=N_PATHS, reps=3)
-    sums = torch.zeros(64, dtype=torch.float64, device="cuda")
-
-    def fused_step():
-        for name, m in models:
-            _lib.check(lib.stocha_price_device(ctx, ctypes.byref(m), seed, _lib.FP32, _lib.PAYOFF_CALL, STRIKE,
-                                               0.05, ctypes.c_void_p(sums.data_ptr())))
+    seed = replica_seed(rank)  # weak scaling: each rank its own independent 1e6 paths per model
 
     def barrier():
         if world > 1:
@@ -585,115 +627,192 @@ def run_ours(args, rank, world):
     def max_over_ranks(x):
         return rank_max(x, world, "cuda")
 
+    models = [(name, stocha.model_struct(name, p, STEPS, N_PATHS)) for name, p in WORKLOAD]
+    width = {"multi_gbm": 3, "heston": 1, "merton": 1}
     path_steps = 3 * N_PATHS * STEPS
-    # ---- headline: FP32 fused, device resident
+    hbm, hbm_src = hbm_peak_gbs()
+
+    # ---- headline: FP64 plain, materialised into device memory ----------
+    bufs64 = [torch.empty((N_PATHS, STEPS + 1, width[n]) if width[n] > 1 else (N_PATHS, STEPS + 1),
+                          dtype=torch.float64, device="cuda") for n, _ in models]
+    bytes64 = sum(b.numel() * 8 for b in bufs64)
+
+    def paths_launch(i, prec, buf):
+        _lib.check(lib.stocha_paths_device(ctx, ctypes.byref(models[i][1]), seed, prec, ctypes.c_void_p(buf.data_ptr())))
+
+    def fp64_step():
+        for i in range(3):
+            paths_launch(i, _lib.FP64, bufs64[i])
+
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
-            fused_step()
+            fp64_step()
         stream.synchronize()
         _lib.check(lib.stocha_ctx_sync(ctx))
         barrier()
         torch.cuda.synchronize()
         with ClockSampler(dev) as clocks:
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            for _ in range(args.steps):
-                fused_step()
-            e1.record(stream)
-            e1.synchronize()
+            ms = _events(stream, fp64_step, args.steps)
             barrier()
             torch.cuda.synchronize()
         _lib.check(lib.stocha_ctx_sync(ctx))
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
-    value = world * path_steps / (ms * 1e-3)
+        ms = max_over_ranks(ms)
+        value = world * path_steps / (ms * 1e-3)
+        # per-model kernel time (3 launches each) for the roofline
+        kms64 = {n: _events(stream, lambda i=i: paths_launch(i, _lib.FP64, bufs64[i]), 3)
+                 for i, (n, _) in enumerate(models)}
+    del bufs64
+    torch.cuda.empty_cache()
+    peak_dfma = ctypes.c_double(0)
+    _lib.check(lib.stocha_measure_peak(ctx, 1, ctypes.byref(peak_dfma)))
+    peak_fp64_ops = peak_dfma.value / 2  # DFMA/s (the kernel reports flop/s, 2 per DFMA)
+    dom = max(kms64, key=kms64.get)
+    ops = FP64_OPS_PER_PATH_STEP[dom] * N_PATHS * STEPS
+    roofline = {
+        "bound": "fp64 pipe", "kernel": f"k_{dom}_f64 (materialised)",
+        "achieved": ops / (kms64[dom] * 1e-3) / 1e9, "peak": peak_fp64_ops / 1e9, "unit": "G FP64 ops/s",
+        "frac": ops / (kms64[dom] * 1e-3) / peak_fp64_ops,
+        "peak_source": "measured live (stocha_measure_peak kind 1, DFMA chains)",
+        "ops_per_path_step": FP64_OPS_PER_PATH_STEP[dom],
+        "kernel_ms": kms64,
+        # the bytes the dominant kernel writes, against the measured HBM copy rate
+        "hbm": {"achieved_gbs": N_PATHS * (STEPS + 1) * width[dom] * 8 / (kms64[dom] * 1e-3) / 1e9,
+                "peak_gbs": hbm, "peak_source": hbm_src},
+        # dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu, profiles/), scaled by rows
+        "traffic": None,
+    }
+    roofline["hbm"]["frac"] = roofline["hbm"]["achieved_gbs"] / hbm
 
-    # per-model kernel time (average of 3 launches) for the roofline
-    per_model = {}
+    # ---- e2e: FP64 plain through the public API into NumPy --------------
+    e2e = None
+    if not args.skip_e2e:
+        corr = np.array(CORR3)
+
+        def e2e_step():
+            # each result is dropped before the next call, as a caller that
+            # reduces the paths and moves on would
+            x = stocha.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, N_PATHS, seed=seed)
+            s = float(x[-1, -1, 0])  # a host read of the result
+            del x
+            x = stocha.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")],
+                              STEPS, N_PATHS, seed=seed)
+            s += float(x[-1, -1])
+            del x
+            x = stocha.merton_jump_diffusion(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j",
+                                                                   "sigma_j", "t")], STEPS, N_PATHS, seed=seed)
+            s += float(x[-1, -1])
+            del x
+            return s
+
+        t0 = time.perf_counter()
+        e2e_step()  # the first call writes into fresh host memory
+        first_s = time.perf_counter() - t0
+        for _ in range(max(0, args.warmup - 1)):
+            e2e_step()
+        barrier()
+        k_e2e = max(1, args.steps // 2) if N_PATHS >= 1_000_000 else args.steps
+        t0 = time.perf_counter()
+        for _ in range(k_e2e):
+            e2e_step()
+        e2e_s = max_over_ranks((time.perf_counter() - t0) / k_e2e)
+        e2e = {"value": world * path_steps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
+               "d2h_bytes_per_step": bytes64, "steps": k_e2e, "ms_per_step": e2e_s * 1e3,
+               "first_call_value": world * path_steps / first_s,
+               "api": "stocha_gb300.multi_gbm / heston / merton_jump_diffusion -> NumPy float64 arrays",
+               "note": "inputs are scalar parameters (kernel arguments); d2h = the three path arrays. The "
+                       "device-to-host link of this box moves 193.6 GB/s by copy engine or SM stores "
+                       "alike (measured), so 10.1 GB take >= 52 ms a step"}
+
+    # ---- FP32 fused pricing (GB300 precision form) ------------------------
+    tuning = {}
+    if not args.no_tune:
+        for name, p in WORKLOAD:
+            tuning[name] = stocha.autotune(name, p, steps=STEPS, n_paths=N_PATHS, reps=3)
+    sums = torch.zeros(64, dtype=torch.float64, device="cuda")
+
+    def price_launch(i, prec):
+        _lib.check(lib.stocha_price_device(ctx, ctypes.byref(models[i][1]), seed, prec, _lib.PAYOFF_CALL, STRIKE,
+                                           0.05, ctypes.c_void_p(sums.data_ptr())))
+
+    fp32f = {}
     with torch.cuda.stream(stream):
-        for name, m in models:
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            for _ in range(3):
-                _lib.check(lib.stocha_price_device(ctx, ctypes.byref(m), seed, _lib.FP32, _lib.PAYOFF_CALL, STRIKE,
-                                                   0.05, ctypes.c_void_p(sums.data_ptr())))
-            b.record(stream)
-            b.synchronize()
-            per_model[name] = a.elapsed_time(b) / 3
+        for _ in range(3):
+            for i in range(3):
+                price_launch(i, _lib.FP32)
+        ms32 = _events(stream, lambda: [price_launch(i, _lib.FP32) for i in range(3)], args.steps)
+        kms32 = {n: _events(stream, lambda i=i: price_launch(i, _lib.FP32), 3) for i, (n, _) in enumerate(models)}
+    ms32 = max_over_ranks(ms32)
     peak_draws = ctypes.c_double(0)
     _lib.check(lib.stocha_measure_peak(ctx, 3, ctypes.byref(peak_draws)))
+    peaks = {}
+    for kind, nm in ((0, "ffma_flops"), (2, "imad_ops")):
+        v = ctypes.c_double(0)
+        _lib.check(lib.stocha_measure_peak(ctx, kind, ctypes.byref(v)))
+        peaks[nm] = v.value
     draws = sum(DRAWS_PER_PATH_STEP[n] * N_PATHS * STEPS for n, _ in WORKLOAD)
-    achieved = draws / (sum(per_model.values()) * 1e-3)
+    achieved_draws = draws / (sum(kms32.values()) * 1e-3)
+    fp32f = {"value": world * path_steps / (ms32 * 1e-3), "unit": "path-steps/s", "ms_per_step": ms32,
+             "speedup_vs_fp64_plain": (world * path_steps / (ms32 * 1e-3)) / value,
+             "kernel_ms": kms32, "autotune": tuning,
+             "roofline": {"bound": "integer pipes and issue (PCG64DXSM generator)",
+                          "achieved": achieved_draws / 1e9, "unit": "G draws/s",
+                          "generator_alone_peak": peak_draws.value / 1e9,
+                          "frac_of_generator_alone": achieved_draws / peak_draws.value,
+                          "peak_source": "measured live (stocha_measure_peak kind 3)",
+                          "measured_pipe_peaks": {"ffma_gflops": peaks["ffma_flops"] / 1e9,
+                                                  "imad_gops": peaks["imad_ops"] / 1e9,
+                                                  "dfma_gflops": peak_dfma.value / 1e9},
+                          "traffic": 77824, "traffic_unit": "bytes per launch (multi-GBM kernel: tables only)"},
+             "config": "same three models, 1e6 paths x 252 steps, European call K=100 reduced in-kernel, FP32 "
+                       "paths (<= 1e-4 relative price error vs FP64)"}
+    if not args.skip_e2e:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for name, p in WORKLOAD:
+                stocha.price_european(name, p, STRIKE, steps=STEPS, n_paths=N_PATHS, seed=seed, precision="fp32",
+                                      rate=0.05)
+        e2e32 = max_over_ranks((time.perf_counter() - t0) / args.steps)
+        fp32f["e2e"] = {"value": world * path_steps / e2e32, "unit": "path-steps/s", "h2d_bytes_per_step": 3 * 4096,
+                        "d2h_bytes_per_step": 8 * (6 + 2 + 2),
+                        "api": "stocha_gb300.price_european(precision='fp32') -> (price, std_err)"}
 
-    # ---- e2e FP32 fused through the public API
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(0 if args.skip_e2e else args.steps):
-        for name, p in WORKLOAD:
-            stocha.price_european(name, p, STRIKE, steps=STEPS, n_paths=N_PATHS, seed=seed, precision="fp32",
-                                  rate=0.05)
-    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps)
-    e2e = world * path_steps / e2e_s if not args.skip_e2e else None
-
-    # ---- FP64 plain: materialised paths, device resident and end to end
-    fp64 = {}
-    if not args.skip_fp64:
-        bufs = [torch.empty((N_PATHS, STEPS + 1, 3), dtype=torch.float64, device="cuda"),
-                torch.empty((N_PATHS, STEPS + 1), dtype=torch.float64, device="cuda"),
-                torch.empty((N_PATHS, STEPS + 1), dtype=torch.float64, device="cuda")]
-
-        def fp64_step():
-            for (name, m), b in zip(models, bufs):
-                _lib.check(lib.stocha_paths_device(ctx, ctypes.byref(m), seed, _lib.FP64, ctypes.c_void_p(b.data_ptr())))
-
-        k64 = max(1, min(args.steps, 3))
-        with torch.cuda.stream(stream):
-            fp64_step()
-            stream.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            for _ in range(k64):
-                fp64_step()
-            b.record(stream)
-            b.synchronize()
-            _lib.check(lib.stocha_ctx_sync(ctx))
-        ms64 = max_over_ranks(a.elapsed_time(b) / k64)
-        del bufs
-        torch.cuda.empty_cache()
-        fp64 = {"value": world * path_steps / (ms64 * 1e-3), "ms_per_step": ms64, "steps": k64,
-                "bytes_written_per_step": 8 * N_PATHS * (STEPS + 1) * 5}
-        if not args.skip_e2e64:
-            corr = np.array(CORR3)
-
-            def e2e64_pass():
-                # each result is dropped before the next call, as a caller that
-                # reduces the paths and moves on would
-                t0 = time.perf_counter()
-                x = stocha.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, N_PATHS, seed=seed)
-                del x
-                x = stocha.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")],
-                                  STEPS, N_PATHS, seed=seed)
-                del x
-                x = stocha.merton_jump_diffusion(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j",
-                                                                       "sigma_j", "t")], STEPS, N_PATHS, seed=seed)
-                del x
-                return max_over_ranks(time.perf_counter() - t0)
-
-            # the first pass writes into fresh host memory; later passes reuse the
-            # host result cache's buffers, whose pages already exist
-            cold = e2e64_pass()
-            warm = min(e2e64_pass() for _ in range(2))
-            fp64["e2e"] = {"value": world * path_steps / warm, "unit": "path-steps/s",
-                           "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 8 * N_PATHS * (STEPS + 1) * 5,
-                           "first_call_value": world * path_steps / cold}
-        fp64["fp32_fused_speedup"] = value / fp64["value"]
-        hbm, hbm_src = hbm_peak_gbs()
-        gbs = fp64["bytes_written_per_step"] / (ms64 * 1e-3) / 1e9
-        fp64["roofline"] = {"bound": "FP64 pipe (Heston) and issue (the others); not HBM, see profiles/",
-                            "achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm,
-                            "peak_source": hbm_src, "note": "algorithmic bytes = the materialised paths written"}
-        fp64["form"] = ("reference algorithm in FP64 (paths within 1e-12 of the oracle); its exponential, the "
-                        "Heston sqrt and the normals' products run on the integer pipes (GB300 issues FP64 at "
-                        "1/64 of FP32), 2.7x the FP64-pipe form against which the FP32 fused form was 9.7x")
+    # ---- the other two cells of the configuration: FP64 fused, FP32 materialised
+    with torch.cuda.stream(stream):
+        for i in range(3):
+            price_launch(i, _lib.FP64)
+        k64f = max(1, min(args.steps, 5))
+        ms64f = _events(stream, lambda: [price_launch(i, _lib.FP64) for i in range(3)], k64f)
+        kms64f = {n: _events(stream, lambda i=i: price_launch(i, _lib.FP64), 2) for i, (n, _) in enumerate(models)}
+    ms64f = max_over_ranks(ms64f)
+    d64f = max(kms64f, key=kms64f.get)
+    ops_f = FP64_OPS_PER_PATH_STEP[d64f] * N_PATHS * STEPS
+    fp64_fused = {"value": world * path_steps / (ms64f * 1e-3), "unit": "path-steps/s", "ms_per_step": ms64f,
+                  "steps": k64f, "kernel_ms": kms64f,
+                  "roofline": {"bound": "fp64 pipe", "kernel": f"k_{d64f}_f64 (fused)",
+                               "achieved": ops_f / (kms64f[d64f] * 1e-3) / 1e9, "peak": peak_fp64_ops / 1e9,
+                               "unit": "G FP64 ops/s", "frac": ops_f / (kms64f[d64f] * 1e-3) / peak_fp64_ops}}
+    bufs32 = [torch.empty((N_PATHS, STEPS + 1, width[n]) if width[n] > 1 else (N_PATHS, STEPS + 1),
+                          dtype=torch.float32, device="cuda") for n, _ in models]
+    bytes32 = sum(b.numel() * 4 for b in bufs32)
+    with torch.cuda.stream(stream):
+        for i in range(3):
+            paths_launch(i, _lib.FP32, bufs32[i])
+        k32m = max(1, min(args.steps, 5))
+        ms32m = _events(stream, lambda: [paths_launch(i, _lib.FP32, bufs32[i]) for i in range(3)], k32m)
+        kms32m = {n: _events(stream, lambda i=i: paths_launch(i, _lib.FP32, bufs32[i]), 2)
+                  for i, (n, _) in enumerate(models)}
+    _lib.check(lib.stocha_ctx_sync(ctx))
+    ms32m = max_over_ranks(ms32m)
+    del bufs32
+    torch.cuda.empty_cache()
+    gbs32 = bytes32 / (ms32m * 1e-3) / 1e9
+    fp32_mat = {"value": world * path_steps / (ms32m * 1e-3), "unit": "path-steps/s", "ms_per_step": ms32m,
+                "steps": k32m, "kernel_ms": kms32m, "bytes_written_per_step": bytes32,
+                "roofline": {"bound": "integer pipes and issue (generator); HBM is not reached",
+                             "hbm_achieved_gbs": gbs32, "hbm_peak_gbs": hbm, "hbm_frac": gbs32 / hbm,
+                             "peak_source": hbm_src,
+                             "generator_floor_ms": draws / peak_draws.value * 1e3,
+                             "hbm_floor_ms": bytes32 / (hbm * 1e9) * 1e3}}
 
     extras = {}
     if rank == 0 and not args.skip_extras:
@@ -705,35 +824,23 @@ def run_ours(args, rank, world):
         sample = 20_000
         cpu_baseline(cores, 2000)
         cpu = {"value": cpu_baseline(cores, sample), "unit": "path-steps/s", "cores": cores, "kind": "port",
-               "sample": f"{sample} paths x {STEPS} steps per model (3 models), FP64 materialised + payoff"}
+               "sample": f"{sample} paths x {STEPS} steps per model (3 models), FP64 paths gathered into host "
+                         "arrays (the oracle, all host cores)"}
 
     if rank == 0:
         line = {
             "metric": "path-steps/s", "value": value, "unit": "path-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; reference parameters)",
-            "config": {"workload": "multi_gbm(3 assets, corr [[1,.6,.3],[.6,1,.5],[.3,.5,1]]) + heston(euler) + "
-                                   "merton(lambda=1, mu_j=-0.05, sigma_j=0.1); 252 steps; 1e6 paths each; "
-                                   "european call K=100; FP32 fused",
-                       "paths_per_model": N_PATHS, "steps": STEPS, "seed": seed,
-                       "l2": "no input data (parameters only); FP64 outputs (10.1 GB/step) exceed L2"},
-            "e2e": {"value": e2e, "unit": "path-steps/s", "h2d_bytes_per_step": 3 * 4096,
-                    "d2h_bytes_per_step": 8 * (6 + 2 + 2)},
-            "gpu_launches": 6 * args.steps,
-            "roofline": {"bound": "int (PCG64DXSM generator)", "achieved": achieved / 1e9, "peak": peak_draws.value / 1e9,
-                         "unit": "Gdraws/s", "frac": achieved / peak_draws.value,
-                         # dram__bytes_read.sum + dram__bytes_write.sum of one k_gbm_uf<3> launch
-                         # (ncu, profiles/k_gbm_uf3_fused_200k.md): the staged ziggurat tables only,
-                         # the same at any path count (no path data leaves the registers)
-                         "traffic": 77824, "traffic_unit": "bytes per launch (multi-GBM kernel)",
-                         # that traffic over the kernel's time, against the measured HBM rate: the
-                         # fused form is not memory-bound
-                         "hbm_frac": 77824 / (per_model["multi_gbm"] * 1e-3) / (hbm_peak_gbs()[0] * 1e9),
-                         "kernel_ms": per_model, "peak_source": "measured live (stocha_measure_peak kind 3)"},
-            "fp64_plain": fp64,
-            "autotune": tuning,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference parameters)",
+            "config": headline_config(seed),
+            "e2e": e2e,
+            "gpu_launches": 3 * args.steps,
+            "roofline": roofline,
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
+            "fp32_fused": fp32f,
+            "fp64_fused": fp64_fused,
+            "fp32_materialised": fp32_mat,
         }
         line.update(extras)
         print(json.dumps(line), flush=True)
@@ -747,8 +854,6 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--skip-fp64", action="store_true")
-    ap.add_argument("--skip-e2e64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-extras", action="store_true", help="only the headline workload")
