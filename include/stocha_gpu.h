@@ -112,6 +112,18 @@ int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n);
  * pipes, 3 the same product by the FP64 pipe (they must agree bit for bit),
  * 4 exp in the early-exit form (bit for bit the same as 0). */
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n);
+/* Diagnostic (no counterpart in the reference): the device samplers' iteration
+ * caps.  Thread i < n draws once from the stream of path i (seed advanced by
+ * i * 2050 draws, as a one-step gbm) into out[i] (host buffer), with one cap
+ * lowered to `cap`: sampler 0 FP64 normal attempts, 1 FP64 normal tail
+ * iterations, 2 FP32 normal attempts, 3 FP32 normal tail iterations, 4 gamma
+ * (shape 2.5) rejections.  The reference's loops have no cap
+ * (src/dist/normal.rs:54-67, src/copula/student_t.rs:93-119); the engine's
+ * stop at 4096 (normals) and 2^20 (gamma), set an error bit and return.  A
+ * draw that reaches the cap makes the call return STOCHA_ERR_DEVICE with the
+ * cap named in stocha_last_error(); the next call starts clean. */
+int stocha_debug_capped_draws(stocha_ctx* ctx, int32_t sampler, int32_t cap, uint64_t seed, uint64_t n,
+                              double* out);
 /* Diagnostic (no counterpart in the reference): measured peak rate of one
  * pipe for roofline denominators.  kind 0: FP32 FFMA flop/s, 1: FP64 DFMA
  * flop/s, 2: 32-bit IMAD op/s, 3: PCG64DXSM draws/s (generator alone). */

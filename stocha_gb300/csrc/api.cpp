@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "exp_table.inc"
+#include "copula_t_kernels.h"
 #include "host_common.h"
 #include "ziggurat_table.inc"
 
@@ -187,6 +188,7 @@ int finish_call(stocha_ctx* c) {
     if (e & kErrZigAttempts) what += " normal-draw attempt cap reached;";
     if (e & kErrTailIters) what += " ziggurat tail iteration cap reached;";
     if (e & kErrQueue) what += " work-queue inconsistency;";
+    if (e & kErrGammaIters) what += " gamma rejection cap reached;";
     return set_error(STOCHA_ERR_DEVICE, "device check failed:" + what);
   }
   return STOCHA_OK;
@@ -436,6 +438,16 @@ void fill_f32_constants(PathLaunch* L) {
   f.h_nhdt = (float)(-0.5 * h.dt);
   f.h_mudt = (float)(h.mu * h.dt);
   f.h_sdt = (float)h.sqrt_dt;
+  f.q_ekdt = (float)h.e_kdt;
+  f.q_m0 = (float)h.qe_m0;
+  f.q_cs2 = h.kappa > 0.0 ? (float)(h.xi * h.xi * h.e_kdt * h.one_m_ekdt / h.kappa) : 0.0f;
+  f.q_s2b = (float)h.qe_s2b;
+  f.q_k0 = (float)h.k0_s;
+  f.q_k1 = (float)h.k1_s;
+  f.q_k2 = (float)h.k2_s;
+  f.q_k3 = (float)h.k3_s;
+  f.q_k4 = (float)h.k4_s;
+  f.q_ls0 = h.s0 > 0.0 ? (float)std::log(h.s0) : 0.0f;
   for (int i = 0; i < kMaxAssets; ++i) {
     f.a_s0[i] = (float)L->multi.s0[i];
     f.a_kdrift[i] = (float)(steps * L->multi.drift[i]);
@@ -781,6 +793,35 @@ int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n) {
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n) {
   if (fn < 0 || fn > 4) return set_error(STOCHA_ERR_VALUE, "fn must be 0..4");
   return debug_f64(fn, ctx, x, y, n);
+}
+
+int stocha_debug_capped_draws(stocha_ctx* ctx, int32_t sampler, int32_t cap, uint64_t seed, uint64_t n,
+                              double* out) {
+  if (sampler < 0 || sampler > 4) return set_error(STOCHA_ERR_VALUE, "sampler must be 0..4");
+  if (cap < 1) return set_error(STOCHA_ERR_VALUE, "cap must be positive");
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  if (n == 0) return STOCHA_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if ((rc = ensure_buf(ctx, ctx->aux, n * sizeof(double)))) return rc;
+  DebugCapped a;
+  std::memset(&a, 0, sizeof a);
+  make_stream_spec((u128)seed, (u128)(1 + 1024) * 2, &a.ss);  // one-step GBM streams (gbm.rs:55)
+  a.tabs = ctx->d_tabs;
+  a.err = ctx->d_err;
+  a.out = (double*)ctx->aux.ptr;
+  a.n = n;
+  a.sampler = sampler;
+  a.cap = cap;
+  // gamma of shape nu / 2 = 2.5 (nu = 5), Marsaglia-Tsang: d = shape - 1/3, c = 1 / sqrt(9 d)
+  a.d = 2.5 - 1.0 / 3.0;
+  a.c = 1.0 / std::sqrt(9.0 * a.d);
+  if ((rc = begin_call(ctx))) return rc;
+  launch_debug_capped(a, ctx->stream);
+  STOCHA_CUDA(cudaGetLastError());
+  STOCHA_CUDA(cudaMemcpyAsync(out, a.out, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  return finish_call(ctx);
 }
 
 int stocha_debug_zig_thresholds(uint64_t* thr256) {

@@ -20,19 +20,23 @@
 // coefficients).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "copula_t_kernels.h"
 #include "mc_device.cuh"
 
 namespace stocha {
 namespace {
 
-__device__ __forceinline__ double next_f64(CountingGen& g) { return u64_to_unit_f64(g.next()); }  // pcg64.rs:37-39
+template <class G>
+__device__ __forceinline__ double next_f64(G& g) { return u64_to_unit_f64(g.next()); }  // pcg64.rs:37-39
 
 // student_t.rs:93-119 (shape >= 1: nu > 2 is enforced)
-__device__ double sample_gamma(CountingGen& g, double d, double c, const SamplerCtx& sc, const ZigShared& zs,
-                               unsigned& err) {
+template <class G>
+__device__ double sample_gamma(G& g, double d, double c, const SamplerCtx& sc, const ZigShared& zs, unsigned& err,
+                               int max_iter = kGammaMaxIters) {
 #pragma unroll 1
-  for (int it = 0; it < 1 << 20; ++it) {
+  for (int it = 0; it < max_iter; ++it) {
     const double x = normal_f64(g, sc, zs, err);
     const double v_inner = 1.0 + c * x;
     if (v_inner <= 0.0) continue;
@@ -41,7 +45,7 @@ __device__ double sample_gamma(CountingGen& g, double d, double c, const Sampler
     if (u < 1.0 - 0.0331 * (x * x) * (x * x)) return d * v;
     if (log(u) < 0.5 * x * x + d * (1.0 - v + log(v))) return d * v;
   }
-  err |= kErrZigAttempts;
+  err |= kErrGammaIters;
   return d;
 }
 
@@ -274,6 +278,26 @@ __global__ void __launch_bounds__(256) k_tcdf(const double* __restrict__ raw, co
   }
 }
 
+__global__ void __launch_bounds__(256) k_debug_capped(const __grid_constant__ DebugCapped a) {
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, true);
+  const SamplerCtx sc{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (uint64_t)gridDim.x * blockDim.x) {
+    PcgGen g{pcg_path_state(a.ss, i), a.ss.inc_lo, a.ss.inc_hi};
+    double v;
+    switch (a.sampler) {
+      case 0: v = normal_f64(g, sc, zs, err, a.cap, kZigMaxTail); break;
+      case 1: v = normal_f64(g, sc, zs, err, kZigMaxAttempts, a.cap); break;
+      case 2: v = normal_f32(g, sc, zs, err, nullptr, a.cap, kZigMaxTail); break;
+      case 3: v = normal_f32(g, sc, zs, err, nullptr, kZigMaxAttempts, a.cap); break;
+      default: v = sample_gamma(g, a.d, a.c, sc, zs, err, a.cap); break;
+    }
+    a.out[i] = v;
+  }
+  if (err) atomicOr(a.err, err);
+}
+
 }  // namespace
 
 void launch_tparse(const TParse& a, cudaStream_t st) {
@@ -301,6 +325,10 @@ void launch_tcdf(const double* raw, const double* L, uint64_t n, int dim, double
   uint64_t g = (total + 255) / 256;
   if (g > 152ull * 32) g = 152ull * 32;
   k_tcdf<<<(unsigned)(g ? g : 1), 256, 0, st>>>(raw, L, n, dim, nu, log_beta, cf, u);
+}
+
+void launch_debug_capped(const DebugCapped& a, cudaStream_t st) {
+  if (a.n) k_debug_capped<<<(unsigned)std::min<uint64_t>((a.n + 255) / 256, 4096), 256, 0, st>>>(a);
 }
 
 }  // namespace stocha

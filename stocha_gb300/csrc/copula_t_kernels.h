@@ -31,6 +31,22 @@ struct TParse {
   uint64_t* gfirst;     // ngroups: index of the group's first sample
 };
 
+// Diagnostic: thread i < n draws once from path i's stream (ss: block-split
+// streams) with the engine's samplers and a lowered iteration cap, so that
+// the caps' error path can be driven: sampler 0 FP64 normal (attempt cap),
+// 1 FP64 normal (tail cap), 2 FP32 normal (attempt cap), 3 FP32 normal (tail
+// cap), 4 gamma of shape nu / 2 with constants (d, c) (rejection cap).
+struct DebugCapped {
+  StreamSpec ss;
+  const ZigTables* tabs;
+  unsigned* err;
+  double* out;
+  uint64_t n;
+  int sampler, cap;
+  double d, c;
+};
+void launch_debug_capped(const DebugCapped& a, cudaStream_t st);
+
 void launch_tparse(const TParse& a, cudaStream_t st);
 void launch_tstitch(const TParse& a, cudaStream_t st);
 void launch_temit(const TParse& a, const uint64_t* status, cudaStream_t st);

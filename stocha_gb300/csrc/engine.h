@@ -49,6 +49,9 @@ struct F32K {
   float g_s0, g_kdrift, g_diff, g_drift;  // GBM: kdrift = steps * drift
   float m_s0, m_kdrift, m_diff, m_drift, m_mu_j, m_sigma_j;  // Merton
   float h_s0, h_v0, h_rho, h_rho_comp, h_kdt, h_theta, h_xsdt, h_nhdt, h_mudt, h_sdt;  // Heston Euler
+  // Heston QE: m = m0 + v+ e_kdt, s2 = cs2 v+ + s2b, log-price coefficients
+  // k0..k4 (heston.rs:112-150), log s0
+  float q_ekdt, q_m0, q_cs2, q_s2b, q_k0, q_k1, q_k2, q_k3, q_k4, q_ls0;
   float a_s0[kMaxAssets], a_kdrift[kMaxAssets], a_diff[kMaxAssets], a_drift[kMaxAssets];
   float a_L[kMaxAssets * kMaxAssets];
 };

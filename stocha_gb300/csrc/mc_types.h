@@ -46,11 +46,13 @@ enum : unsigned {
   kErrZigAttempts = 1u,  // a normal draw exceeded the rejection-attempt cap
   kErrTailIters = 2u,    // a ziggurat tail draw exceeded its iteration cap
   kErrQueue = 4u,        // persistent work queue inconsistency
+  kErrGammaIters = 8u,   // a gamma draw exceeded its rejection cap
 };
 
 // Iteration caps for rejection loops.  The reference loops without bound; the
 // probability of reaching these caps with a correct table is below 1e-300.
 constexpr int kZigMaxAttempts = 4096;
 constexpr int kZigMaxTail = 4096;
+constexpr int kGammaMaxIters = 1 << 20;
 
 }  // namespace stocha

@@ -346,6 +346,81 @@ __global__ void __launch_bounds__(256, kMode != kFused ? 1 : kFusedMinBlocks) k_
   if (err) atomicOr(a.err, err);
 }
 
+// Heston QE (heston.rs:89-174) in FP32: the same branches and the same draws
+// as the FP64 form (a normal in the quadratic branch, one uniform in the
+// exponential one, then the log-price normal), v in FP32 and the log price
+// carried as a running sum with the reference's clamp to [-500, 500].  A
+// branch decision psi <= 1.5 computed in FP32 can differ from FP64's for psi
+// within ~1e-6 of 1.5; that path then draws differently from there on (a
+// valid path of the same scheme), which is rare enough to stay inside the
+// FP32 price bar.
+template <int kMode>
+__global__ void __launch_bounds__(256, kMode != kFused ? 1 : kFusedMinBlocks) k_heston_qe_f32(const __grid_constant__ PathLaunch a) {
+  constexpr bool kStore = kMode != kFused;
+  PathOut<float, kMode> out;
+  out.init(dyn_smem);
+  __shared__ ZigShared zs;
+  zig_stage(zs, a.tabs, false);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  unsigned err = 0;
+  auto path = [&](uint64_t lrow, float* pay) {
+    const uint64_t row = a.row_begin + lrow;
+    PcgGen s{pcg_path_state(a.ss, row), a.ss.inc_lo, a.ss.inc_hi};
+    float v = f.h_v0;
+    PathSum<kStore> lg;
+    lg.add(f.q_ls0);
+    if (kMode == kRows) out.begin(a.out_f32 + lrow * (a.steps + 1));
+    if (kStore) emit32(out, a, lrow, 0, 1, 0, f.h_s0);
+#pragma unroll 1
+    for (uint64_t k = 1; k <= a.steps; ++k) {
+      const float vp = fmaxf(v, 0.0f);
+      const float m = fmaxf(fmaf(vp, f.q_ekdt, f.q_m0), 1e-15f);
+      const float s2 = fmaf(vp, f.q_cs2, f.q_s2b);
+      const float psi = s2 / (m * m);
+      float vn;
+      if (psi <= 1.5f) {  // quadratic branch: V ~ a (b + Z)^2
+        const float ip = 2.0f / psi;
+        const float b2 = fmaxf(ip - 1.0f + sqrtf(ip * (ip - 1.0f)), 0.0f);
+        const float aa = m / (1.0f + b2);
+        const float b = sqrtf(b2);
+        const float z = normal_f32(s, c, zs, err);
+        vn = aa * (b + z) * (b + z);
+      } else {  // exponential branch: point mass at 0 and an exponential
+        const float p = (psi - 1.0f) / (psi + 1.0f);
+        const float beta = (1.0f - p) / m;
+        const uint64_t mu = s.next() >> 11;  // next_f64 = mu 2^-53
+        // 1 - u from the integer, so it is never rounded to 0
+        const float one_m_u = __ull2float_rn((1ull << 53) - mu) * 0x1p-53f;
+        vn = __ull2float_rn(mu) * 0x1p-53f <= p ? 0.0f : logf((1.0f - p) / one_m_u) / beta;
+      }
+      vn = fmaxf(vn, 0.0f);
+      const float z1 = normal_f32(s, c, zs, err);
+      const float var = fmaxf(fmaf(f.q_k3, vp, f.q_k4 * vn), 0.0f);
+      lg.add(fmaf(sqrtf(var), z1, fmaf(f.q_k2, vn, fmaf(f.q_k1, vp, f.q_k0))));
+      const float lv = lg.value();
+      if (!(lv <= 500.0f && lv >= -500.0f)) {  // the reference's clamp of log S
+        lg = PathSum<kStore>();
+        lg.add(fminf(fmaxf(lv, -500.0f), 500.0f));
+      }
+      v = vn;
+      if (kStore) emit32(out, a, lrow, k, 1, 0, expf(lg.value()));
+    }
+    if (!kStore) pay[0] = payoff_f32(expf(lg.value()), f.strike, a.payoff);
+  };
+  if constexpr (kStore) {
+    for_rows(a.rows, out, [&](uint64_t lrow) { path(lrow, nullptr); });
+  } else {
+    run_rows<1>(a, [&](uint64_t b, float* p) {
+      const uint64_t lrow = b + (threadIdx.x & 31u);
+      if (lrow >= a.rows) return false;
+      path(lrow, p);
+      return true;
+    });
+  }
+  if (err) atomicOr(a.err, err);
+}
+
 template <int kMode>
 __global__ void __launch_bounds__(256, kMode != kFused ? 1 : kFusedMinBlocks) k_merton_f32(const __grid_constant__ PathLaunch a) {
   constexpr bool kStore = kMode != kFused;
@@ -836,7 +911,8 @@ template <int kMode>
 const void* model_kernel32(const PathLaunch& L) {
   switch (L.model) {
     case kGbm: return (const void*)k_gbm_f32<kMode>;
-    case kHeston: return (const void*)k_heston_euler_f32<kMode>;
+    case kHeston:
+      return L.heston.scheme != 0 ? (const void*)k_heston_qe_f32<kMode> : (const void*)k_heston_euler_f32<kMode>;
     case kMerton: return (const void*)k_merton_f32<kMode>;
     default: return (const void*)k_multi_gbm_f32<3, kMode>;
   }
@@ -847,8 +923,10 @@ int launch_model32(const PathLaunch& L, dim3 G, dim3 B, size_t sm, cudaStream_t 
   switch (L.model) {
     case kGbm: k_gbm_f32<kMode><<<G, B, sm, st>>>(L); break;
     case kHeston:
-      if (L.heston.scheme != 0) return -1;  // QE has no FP32 form
-      k_heston_euler_f32<kMode><<<G, B, sm, st>>>(L);
+      if (L.heston.scheme != 0)
+        k_heston_qe_f32<kMode><<<G, B, sm, st>>>(L);
+      else
+        k_heston_euler_f32<kMode><<<G, B, sm, st>>>(L);
       break;
     case kMerton: k_merton_f32<kMode><<<G, B, sm, st>>>(L); break;
     case kMultiGbm: launch_multi32<kMode>(L, G, B, sm, st); break;

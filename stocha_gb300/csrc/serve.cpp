@@ -223,7 +223,7 @@ int validate(const stocha_request& r) {
   if (x.model != STOCHA_MODEL_GBM && x.model != STOCHA_MODEL_HESTON && x.model != STOCHA_MODEL_MERTON)
     return set_error(STOCHA_ERR_VALUE, "model must be gbm, heston or merton");
   if (x.model == STOCHA_MODEL_HESTON && x.scheme != 0)
-    return set_error(STOCHA_ERR_VALUE, "served Heston requests use the euler scheme (the QE form has no FP32 kernel)");
+    return set_error(STOCHA_ERR_VALUE, "served Heston requests use the euler scheme (the batched serving kernel implements Euler only)");
   if (x.payoff != STOCHA_PAYOFF_CALL && x.payoff != STOCHA_PAYOFF_PUT)
     return set_error(STOCHA_ERR_VALUE, "payoff must be call or put");
   if (x.n_paths == 0 || x.steps == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
