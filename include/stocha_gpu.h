@@ -112,6 +112,12 @@ int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n);
  * pipes, 3 the same product by the FP64 pipe (they must agree bit for bit),
  * 4 exp in the early-exit form (bit for bit the same as 0). */
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n);
+/* Diagnostic (no counterpart in the reference): the error of the device's
+ * hardware logarithm __logf over every normal float x in (0, 1), against
+ * log(x) in FP64: the largest absolute error for x in [0.5, 1) and the
+ * largest relative error for x < 0.5.  The FP32 ziggurat tail test's decision
+ * margin rests on these bounds (an exhaustive scan, about a second). */
+int stocha_debug_fast_log_error(stocha_ctx* ctx, double* abs_err_half_to_one, double* rel_err_below_half);
 /* Diagnostic (no counterpart in the reference): the device samplers' iteration
  * caps.  Thread i < n draws once from the stream of path i (seed advanced by
  * i * 2050 draws, as a one-step gbm) into out[i] (host buffer), with one cap

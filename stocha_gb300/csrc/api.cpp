@@ -68,6 +68,7 @@ void build_tables(ZigTables* t) {
   }
   t->r = STOCHA_ZIG_R_HEX;
   t->r32 = (float)t->r;
+  t->nrinv32 = (float)(-1.0 / t->r);
   static const uint64_t E2[256] = STOCHA_EXP2_Q63_INIT;
   for (int j = 0; j < 256; ++j) t->exp2q[j] = E2[j];
 }
@@ -487,10 +488,12 @@ static int paths_to_device(stocha_ctx* c, const stocha_model* m, uint64_t seed, 
 
 // Materialised results at least this large overlap their copy with compute
 // when the destination is a cached host buffer: at most 8 row chunks of at
-// least 2^18 rows, about 1.7 waves of the FP64 kernels' resident threads (1024
-// per SM on 152 SMs), so each chunk still fills the device.
+// least 2^17 rows, about one wave of the FP64 kernels' resident threads (7
+// blocks of 128 per SM on 152 SMs), so each chunk still fills the device and
+// the first copy starts after one wave.  Chunk rows are multiples of 32, so
+// every chunk starts on a whole warp of rows.
 constexpr size_t kOverlapMin = 64u << 20;
-constexpr uint64_t kOverlapMaxChunks = 8, kOverlapMinRows = 1u << 18;
+constexpr uint64_t kOverlapMaxChunks = 8, kOverlapMinRows = 1u << 17;
 
 static int paths_to_host(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, double* out) {
   // Arguments are validated before any CUDA call (as the reference validates
@@ -517,7 +520,8 @@ static int paths_to_host(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, 
       STOCHA_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
       for (cudaEvent_t& e : ctx->chunk_done) STOCHA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    const uint64_t per = std::max<uint64_t>(kOverlapMinRows, (m->n_paths + kOverlapMaxChunks - 1) / kOverlapMaxChunks);
+    const uint64_t per = (std::max<uint64_t>(kOverlapMinRows, (m->n_paths + kOverlapMaxChunks - 1) / kOverlapMaxChunks) +
+                          31) / 32 * 32;
     const uint64_t nch = (m->n_paths + per - 1) / per;
     for (uint64_t i = 0; i < nch; ++i) {
       const uint64_t r0 = i * per, r1 = std::min<uint64_t>(m->n_paths, r0 + per);
@@ -793,6 +797,27 @@ int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n) {
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n) {
   if (fn < 0 || fn > 4) return set_error(STOCHA_ERR_VALUE, "fn must be 0..4");
   return debug_f64(fn, ctx, x, y, n);
+}
+
+int stocha_debug_fast_log_error(stocha_ctx* ctx, double* abs_err_half_to_one, double* rel_err_below_half) {
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  if ((rc = ensure_buf(ctx, ctx->aux, 2 * sizeof(unsigned)))) return rc;
+  unsigned* d = (unsigned*)ctx->aux.ptr;
+  STOCHA_CUDA(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned), ctx->stream));
+  launch_debug_logf_scan(d, ctx->stream);
+  STOCHA_CUDA(cudaGetLastError());
+  unsigned h[2];
+  STOCHA_CUDA(cudaMemcpyAsync(h, d, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  STOCHA_CUDA(cudaStreamSynchronize(ctx->stream));
+  float a, r;
+  std::memcpy(&a, &h[0], 4);
+  std::memcpy(&r, &h[1], 4);
+  if (abs_err_half_to_one) *abs_err_half_to_one = a;
+  if (rel_err_below_half) *rel_err_below_half = r;
+  return STOCHA_OK;
 }
 
 int stocha_debug_capped_draws(stocha_ctx* ctx, int32_t sampler, int32_t cap, uint64_t seed, uint64_t n,

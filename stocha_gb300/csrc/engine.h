@@ -127,6 +127,9 @@ int launch_paths_f64(const PathLaunch& L, cudaStream_t st);
 int launch_paths_f32(const PathLaunch& L, cudaStream_t st);
 // y[i] = exp(x[i]) by the kernels' table-driven exponential (diagnostic).
 void launch_debug_f64(int fn, const double* x, double* y, uint64_t n, const ZigTables* tabs, cudaStream_t st);
+// out[0..1] (zeroed by the caller): float bits of the largest absolute error
+// of __logf on [0.5, 1) and of its largest relative error below 0.5.
+void launch_debug_logf_scan(unsigned* out, cudaStream_t st);
 // Sum per-block partials (deterministic order) into out[nvals].
 void launch_reduce_partials(const double* partials, int nblocks, int nvals, double* out, cudaStream_t st);
 

@@ -11,6 +11,11 @@
 //   * into fresh memory, the destination's pages are populated by a small
 //     pool of host threads (one write per page) and the copy is issued chunk
 //     by chunk as chunks become ready.
+// A cached buffer is also registered with the driver (cudaHostRegister) when
+// it is first reused.  Copies into unregistered pageable memory pin its pages
+// on the fly, and the driver drops those pins now and then: measured on
+// GB300, one copy of a 6 GB result in five or six took 165-255 ms instead of
+// 34 ms.  Registered once, the buffer keeps its pins while it stays cached.
 #include <atomic>
 #include <condition_variable>
 #include <cstdlib>
@@ -121,14 +126,14 @@ class HostCache {
         const Buf b = free_[best];
         free_.erase(free_.begin() + (std::ptrdiff_t)best);
         cached_ -= b.cap;
-        live_[b.p] = Live{b.cap, true};
+        live_[b.p] = Live{b.cap, true, b.registered};
         return b.p;
       }
     }
     void* p = mmap(nullptr, want, PROT_READ | PROT_WRITE, MAP_PRIVATE | MAP_ANONYMOUS, -1, 0);
     if (p == MAP_FAILED) return nullptr;
     std::lock_guard<std::mutex> lk(mu_);
-    live_[p] = Live{want, false};
+    live_[p] = Live{want, false, false};
     return p;
   }
 
@@ -139,7 +144,7 @@ class HostCache {
       std::lock_guard<std::mutex> lk(mu_);
       auto it = live_.find(p);
       if (it == live_.end()) return false;
-      const Buf b{p, it->second.cap};
+      const Buf b{p, it->second.cap, it->second.registered};
       const bool keep = it->second.populated && b.cap <= cap_;
       live_.erase(it);
       if (keep) {
@@ -154,7 +159,27 @@ class HostCache {
         drop.push_back(b);
       }
     }
-    for (const Buf& b : drop) munmap(b.p, b.cap);
+    for (const Buf& b : drop) {
+      if (b.registered) cudaHostUnregister(b.p);
+      munmap(b.p, b.cap);
+    }
+    return true;
+  }
+
+  // Registers [dst, dst + cap) with the driver if dst is a handed-out buffer
+  // whose pages exist and that is not registered yet; true when it is
+  // registered afterwards.
+  bool register_populated(const void* dst) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = live_.find(const_cast<void*>(dst));
+    if (it == live_.end() || !it->second.populated) return false;
+    if (!it->second.registered) {
+      if (cudaHostRegister(it->first, it->second.cap, cudaHostRegisterPortable) != cudaSuccess) {
+        cudaGetLastError();  // not fatal: the copy still works into pageable memory
+        return false;
+      }
+      it->second.registered = true;
+    }
     return true;
   }
 
@@ -179,10 +204,12 @@ class HostCache {
   struct Buf {
     void* p;
     size_t cap;
+    bool registered;
   };
   struct Live {
     size_t cap;
     bool populated;
+    bool registered;  // cudaHostRegister'ed (pins kept while cached)
   };
   HostCache() {
     page_ = (size_t)sysconf(_SC_PAGESIZE);
@@ -205,11 +232,17 @@ class HostCache {
 
 }  // namespace
 
-bool host_dst_cached(const void* dst, size_t bytes) { return HostCache::get().populated(dst, bytes); }
+bool host_dst_cached(const void* dst, size_t bytes) {
+  HostCache& c = HostCache::get();
+  if (!c.populated(dst, bytes)) return false;
+  c.register_populated(dst);
+  return true;
+}
 
 int copy_to_host_populated(cudaStream_t st, void* dst, const void* src, size_t bytes) {
   HostCache& cache = HostCache::get();
   if (bytes < kParallelMin || cache.populated(dst, bytes)) {
+    if (bytes >= kParallelMin) cache.register_populated(dst);
     STOCHA_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
     cache.mark_populated(dst, bytes);
     return STOCHA_OK;

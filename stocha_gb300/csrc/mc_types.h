@@ -37,7 +37,7 @@ struct ZigTables {
   float y32[257];
   double r;
   float r32;
-  float pad_;
+  float nrinv32;  // -1/R rounded to float (the FP32 tail test's x = ln(u1) * nrinv32)
   uint64_t exp2q[256];  // 2^(j/256) * 2^63 (integer-pipe exponential)
 };
 

@@ -935,6 +935,26 @@ int launch_model32(const PathLaunch& L, dim3 G, dim3 B, size_t sm, cudaStream_t 
   return 0;
 }
 
+// Diagnostic: the error of the hardware logarithm (__logf) over every
+// normal float x in (0, 1), against log(x) in FP64: out[0] the largest
+// absolute error for x in [0.5, 1), out[1] the largest relative error for
+// x < 0.5 (float bits of non-negative values order like the values).  The
+// ziggurat tail test's FP32 margin is derived from these bounds.
+__global__ void __launch_bounds__(256) k_debug_logf_scan(unsigned* out) {
+  float a_max = 0.0f, r_max = 0.0f;
+  const uint32_t lo = 0x00800000u, hi = 0x3F800000u;  // [min normal, 1.0)
+  for (uint32_t b = lo + blockIdx.x * blockDim.x + threadIdx.x; b < hi; b += gridDim.x * blockDim.x) {
+    const float x = __uint_as_float(b);
+    const double d = (double)__logf(x) - log((double)x);
+    if (x >= 0.5f)
+      a_max = fmaxf(a_max, (float)fabs(d));
+    else
+      r_max = fmaxf(r_max, (float)(fabs(d) / -log((double)x)));
+  }
+  atomicMax(out, __float_as_uint(a_max));
+  atomicMax(out + 1, __float_as_uint(r_max));
+}
+
 }  // namespace
 
 int tune_slot(int model, int na) {
@@ -1010,6 +1030,13 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
                                   : launch_model32<kFused>(Ls, G, B, 0, st);
   if (rc < 0) return -1;
   return cudaPeekAtLastError() == cudaSuccess ? (int)g : -1;
+}
+
+void launch_debug_logf_scan(unsigned* out, cudaStream_t st) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  k_debug_logf_scan<<<sms * 8, 256, 0, st>>>(out);
 }
 
 }  // namespace stocha

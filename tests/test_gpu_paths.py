@@ -273,6 +273,25 @@ def test_integer_normal_product_equals_dmul(stocha):
     assert (y_fp[:256] == 0).all() and (y_fp[256:] >= 0).all()
 
 
+def test_fast_log_error_bounds(stocha):
+    """The ziggurat tail test decides in FP32 with the hardware logarithm
+    (__logf) and falls back to FP64 within a margin built from its error
+    bounds, kLogAbs = 5e-7 on [0.5, 1) and kLogRel = 3e-7 |ln x| below 0.5
+    (csrc/mc_device.cuh).  The bounds are checked here over every normal
+    float in (0, 1), the whole domain of the test's arguments, so the FP32
+    decision can never disagree with the reference's FP64 one."""
+    import ctypes
+
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    a, r = ctypes.c_double(), ctypes.c_double()
+    _lib.check(lib.stocha_debug_fast_log_error(None, ctypes.byref(a), ctypes.byref(r)))
+    print(f"__logf: max abs error on [0.5, 1) {a.value:.4g}, max relative error below 0.5 {r.value:.4g}")
+    assert 0 < a.value <= 5e-7, a.value
+    assert 0 < r.value <= 3e-7, r.value
+
+
 def test_host_result_cache_reuse(stocha):
     """A released result's buffer serves the next result of the same size: the
     cached byte count rises on release and falls on reuse, and the values are

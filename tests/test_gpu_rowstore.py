@@ -7,8 +7,8 @@ the row; sectors whose neighbour row is not in the warp (a launch's first or
 last rows, or a launch that does not start on a sector boundary) are written
 element by element.  These tests cover the layouts where that logic has
 cases: row lengths around the two-sector minimum, partial warps, every
-phase of a row within its first sector, multi-asset rows, and chunked
-launches whose base is not sector-aligned.
+phase of a row within its first sector, multi-asset rows, chunked host
+copies, and output buffers that do not start on a sector.
 
 Bars: FP64 paths equal the oracle within PATH_RTOL (the FP64 parity bar);
 FP32 rows are all written (no NaN sentinel left) and within F32_RTOL of the
@@ -58,12 +58,11 @@ def test_multi_gbm_row_layouts(stocha, oracle, na, steps):
     assert _rel(got, want) <= PATH_RTOL
 
 
-def test_chunks_not_sector_aligned(stocha, oracle):
+def test_chunked_host_copy(stocha, oracle):
     """2^21 + 8 rows of 9 doubles into a cached host buffer: the overlap path
-    computes 8 chunks of 262145 rows, so chunk k starts k * 262145 * 9
-    elements into the array, off the 4-element sector grid for odd k.  The
-    result must equal the one-launch result (first call, fresh memory) and
-    the oracle around every chunk boundary."""
+    computes 8 row chunks (multiples of 32 rows) whose copies overlap the
+    next chunk.  The result must equal the one-launch result (first call,
+    fresh memory) and the oracle around every chunk boundary."""
     n, steps = (1 << 21) + 8, 8
     kw = dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=steps, n_paths=n, seed=21)
     a = stocha.gbm(**kw)
@@ -73,12 +72,47 @@ def test_chunks_not_sector_aligned(stocha, oracle):
     gc.collect()
     b = stocha.gbm(**kw)  # the cached buffer: chunked launches
     np.testing.assert_array_equal(b, first)
-    per = (n + 7) // 8
+    per = ((n + 7) // 8 + 31) // 32 * 32
     k = 7 * per + 40
     want = oracle.gbm(100.0, 0.05, 0.2, 1.0, steps, k, seed=21, threads=8)
     for c in range(1, 8):
         lo, hi = c * per - 40, c * per + 40
         assert _rel(b[lo:hi], want[lo:hi]) <= PATH_RTOL, c
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_unaligned_output_base(stocha, precision):
+    """A caller's device buffer need not start on a 32-byte sector: with the
+    output shifted by 1..SE-1 elements every lane-0 row starts mid-sector and
+    the writer stores the unshared pieces element by element.  The values
+    must equal the aligned launch's bit for bit, and nothing outside the
+    array may be written."""
+    torch = pytest.importorskip("torch")
+    from stocha_gb300 import _lib
+
+    lib = _lib.load()
+    se = 4 if precision == "fp64" else 8
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    prec = _lib.FP64 if precision == "fp64" else _lib.FP32
+    n, steps = 1000, 40
+    m = stocha.model_struct("heston", dict(s0=100.0, v0=0.04, mu=0.05, kappa=2.0, theta=0.04, xi=0.3, rho=-0.7,
+                                           t=1.0), steps=steps, n_paths=n)
+    size = n * (steps + 1)
+    base = torch.empty(size + 2 * se, dtype=dt, device="cuda")
+    ref = None
+    for off in range(se):
+        base.fill_(-7.0)
+        view = base[off:off + size]
+        _lib.check(lib.stocha_paths_device(None, ctypes.byref(m), 42, prec, ctypes.c_void_p(view.data_ptr())))
+        _lib.check(lib.stocha_ctx_sync(None))
+        host = base.cpu().numpy()
+        got = host[off:off + size]
+        assert (host[:off] == -7.0).all() and (host[off + size:] == -7.0).all(), off
+        if ref is None:
+            ref = got.copy()
+        else:
+            np.testing.assert_array_equal(got.view(np.uint64 if precision == "fp64" else np.uint32),
+                                          ref.view(np.uint64 if precision == "fp64" else np.uint32))
 
 
 def _paths_device(stocha, torch, model, params, steps, n, precision, seed=42):
