@@ -383,7 +383,10 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
         K.s0[i] = m->s0_v[i];
         K.drift[i] = (m->mu_v[i] - 0.5 * m->sigma_v[i] * m->sigma_v[i]) * dt;
         K.diffusion[i] = m->sigma_v[i] * sqrt_dt;
-        for (int j = 0; j < na; ++j) K.L[i * kMaxAssets + j] = l[i * na + j];
+        for (int j = 0; j < na; ++j) {
+          K.L[i * kMaxAssets + j] = l[i * na + j];
+          K.LD[i * kMaxAssets + j] = K.diffusion[i] * l[i * na + j];
+        }
       }
       if (m->antithetic) L->base_paths = (m->n_paths + 1) / 2;
       *row_len = (m->steps + 1) * (uint64_t)na;

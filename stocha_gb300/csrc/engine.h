@@ -34,7 +34,8 @@ struct MertonK {  // jump_diffusion.rs:49-64
 struct MultiK {  // multi_gbm.rs:22-40
   int na;
   double s0[kMaxAssets], drift[kMaxAssets], diffusion[kMaxAssets];
-  double L[kMaxAssets * kMaxAssets];  // lower Cholesky factor, row-major
+  double L[kMaxAssets * kMaxAssets];   // lower Cholesky factor, row-major
+  double LD[kMaxAssets * kMaxAssets];  // diffusion[i] * L[i][j] (the FP64 kernel's exponent rows)
 };
 
 struct HullWhiteK {  // hull_white.rs:26-30: exact transition constants

@@ -141,26 +141,30 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
     const uint64_t row = a.row_begin + lrow;
     const bool neg = row >= a.base_paths;
     PcgGen s{pcg_path_state(a.ss, neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
-    double sv[NA > 0 ? NA : kMaxAssets], z[NA > 0 ? NA : kMaxAssets], dif[NA > 0 ? NA : kMaxAssets];
+    double sv[NA > 0 ? NA : kMaxAssets], z[NA > 0 ? NA : kMaxAssets];
+    // the antithetic path's -z as a sign flip of each normal (integer XOR, exact)
+    const long long zsgn = neg ? (long long)(1ull << 63) : 0ll;
     if (kMode == kRows) out.begin(a.out_f64 + lrow * (a.steps + 1) * na);
 #pragma unroll
     for (int i = 0; i < na; ++i) {
       sv[i] = a.multi.s0[i];
-      // antithetic sign on the coefficient: L(-z) = -(L z) exactly
-      dif[i] = neg ? -a.multi.diffusion[i] : a.multi.diffusion[i];
       if (kStore) emit64(out, a, lrow, 0, na, i, sv[i]);
     }
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
 #pragma unroll
-      for (int i = 0; i < na; ++i) z[i] = normal_f64<true>(s, c, zs, err);  // FP64-pipe bound: integer products
+      for (int i = 0; i < na; ++i)  // FP64-pipe bound: integer products
+        z[i] = __longlong_as_double(__double_as_longlong(normal_f64<true>(s, c, zs, err)) ^ zsgn);
 #pragma unroll
       for (int i = 0; i < na; ++i) {
-        // row i of L z, one rounding per term
-        double eps = a.multi.L[i * kMaxAssets] * z[0];
+        // exponent drift_i + diffusion_i (L z)_i as one DFMA chain over row i of
+        // diffusion_i L, started from the drift: i + 1 FP64 operations where
+        // the row sum and its scaling took i + 2 (the roundings move by an
+        // ulp or so of the exponent, ~1e-18 of the price per step)
+        double t = fma(a.multi.LD[i * kMaxAssets], z[0], a.multi.drift[i]);
 #pragma unroll
-        for (int m = 1; m <= i; ++m) eps = fma(a.multi.L[i * kMaxAssets + m], z[m], eps);
-        sv[i] = mul_exp(sv[i], fma(dif[i], eps, a.multi.drift[i]), zs);
+        for (int m = 1; m <= i; ++m) t = fma(a.multi.LD[i * kMaxAssets + m], z[m], t);
+        sv[i] = mul_exp(sv[i], t, zs);
         if (kStore) emit64(out, a, lrow, k, na, i, sv[i]);
       }
     }

@@ -152,3 +152,26 @@ def test_greeks_batch_mixed(stocha):
         for j, g in enumerate(ALL):
             assert _close(b64[i, 2 + j], one[g], GREEK_FP64_RTOL), (i, g)
         assert _close(b32[i, 0], b64[i, 0], 1e-4, atol=1e-5), (i, b32[i, 0], b64[i, 0])
+
+
+# configuration 4's FP32 batch against FP64, per Greek, as
+# |fp32 - fp64| / max(|fp64|, 1e-3); measured maxima over the 128 instances:
+# price 1.3e-6, delta 1.0e-6, gamma 4.8e-6, vega 2.8e-5, theta 2.8e-5, rho 1.6e-6
+CONFIG4_BARS = {"price": 1e-5, "delta": 1e-5, "gamma": 1e-4, "vega": 2e-4, "theta": 2e-4, "rho": 1e-5}
+
+
+@pytest.mark.slow
+def test_config4_batch_fp32_against_fp64(stocha):
+    """The 512 seeded Greeks instances of configuration 4 in one FP32 launch;
+    every 4th instance (128) revalued scenario by scenario in FP64."""
+    from bench import greeks_instances
+
+    insts = greeks_instances()
+    assert len(insts) == 512
+    g32 = stocha.greeks_batch(insts, precision="fp32")
+    sample = list(range(0, 512, 4))
+    g64 = stocha.greeks_batch([insts[i] for i in sample], precision="fp64")
+    cols = {"price": 0, "delta": 2, "gamma": 3, "vega": 4, "theta": 5, "rho": 6}
+    for name, j in cols.items():
+        err = np.abs(g32[sample, j] - g64[:, j]) / np.maximum(np.abs(g64[:, j]), 1e-3)
+        assert err.max() <= CONFIG4_BARS[name], (name, float(err.max()), int(np.argmax(err)))
