@@ -528,6 +528,22 @@ def headline_config(seed=SEED):
             "l2": "no input data (parameters only); the 10.1 GB of FP64 paths written per step exceed L2"}
 
 
+# Algorithmic FLOPs per path-step (exp, sqrt and ln counted as 1 each; RNG
+# integer work excluded), frozen with the workload definition: multi-GBM(3)
+# 6 lower-triangular MACs (12) + 3 x (FMA 2, exp 1, mul 1); Heston Euler ~21;
+# Merton ~7; GBM 4.
+FLOPS_PER_PATH_STEP = {"multi_gbm": 24.0, "heston": 21.0, "merton": 7.0, "gbm": 4.0}
+
+# dram__bytes_read.sum + dram__bytes_write.sum per path row of the materialised
+# FP64 kernels, from ncu captures of 2e5-path launches
+# (profiles/k_multi_gbm_heston_f64_rows_200k.md,
+# profiles/rowstore_paths_materialised_200k.md); the traffic is the written
+# rows, so it scales with the row count.  Dirty data still in L2 when a
+# capture ends is not counted, so these sit slightly below the algorithmic
+# 8 * 253 * width bytes a row.
+DRAM_BYTES_PER_ROW = {"multi_gbm": (179.968e3 + 1160.567e6) / 2e5, "heston": (104.960e3 + 351.270e6) / 2e5,
+                      "merton": (0.15e6 + 348.2e6) / 2e5}
+
 # FP64 pipe operations per path-step that each FP64 plain kernel issues
 # (DMUL, DADD, DFMA counted once), read from the kernels: the exponential,
 # the sqrt, the conversions and (multi-GBM, Heston) the normals' products run
@@ -676,19 +692,26 @@ def run_ours(args, rank, world):
     _lib.check(lib.stocha_measure_peak(ctx, 1, ctypes.byref(peak_dfma)))
     peak_fp64_ops = peak_dfma.value / 2  # DFMA/s (the kernel reports flop/s, 2 per DFMA)
     dom = max(kms64, key=kms64.get)
+    flops = FLOPS_PER_PATH_STEP[dom] * N_PATHS * STEPS
     ops = FP64_OPS_PER_PATH_STEP[dom] * N_PATHS * STEPS
     roofline = {
-        "bound": "fp64 pipe", "kernel": f"k_{dom}_f64 (materialised)",
-        "achieved": ops / (kms64[dom] * 1e-3) / 1e9, "peak": peak_fp64_ops / 1e9, "unit": "G FP64 ops/s",
-        "frac": ops / (kms64[dom] * 1e-3) / peak_fp64_ops,
-        "peak_source": "measured live (stocha_measure_peak kind 1, DFMA chains)",
-        "ops_per_path_step": FP64_OPS_PER_PATH_STEP[dom],
+        "bound": "fp64 pipe (and issue)", "kernel": f"k_{dom}_f64 (materialised)",
+        "achieved": flops / (kms64[dom] * 1e-3) / 1e9, "peak": peak_dfma.value / 1e9, "unit": "GFLOP/s",
+        "frac": flops / (kms64[dom] * 1e-3) / peak_dfma.value,
+        "peak_source": "measured live (stocha_measure_peak kind 1: DFMA chains, 2 FLOP each)",
+        "flops_per_path_step": FLOPS_PER_PATH_STEP[dom],
+        # the FP64-pipe operations the kernel issues (the exponential, the
+        # conversions and the normals' products run on the integer pipes)
+        "issued_fp64_ops_per_path_step": FP64_OPS_PER_PATH_STEP[dom],
+        "issued_fp64_pipe_frac": ops / (kms64[dom] * 1e-3) / peak_fp64_ops,
         "kernel_ms": kms64,
         # the bytes the dominant kernel writes, against the measured HBM copy rate
         "hbm": {"achieved_gbs": N_PATHS * (STEPS + 1) * width[dom] * 8 / (kms64[dom] * 1e-3) / 1e9,
                 "peak_gbs": hbm, "peak_source": hbm_src},
-        # dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu, profiles/), scaled by rows
-        "traffic": None,
+        # dram__bytes_read.sum + dram__bytes_write.sum per launch (ncu on 2e5 rows, scaled by rows)
+        "traffic": DRAM_BYTES_PER_ROW[dom] * N_PATHS,
+        "traffic_unit": "bytes per launch",
+        "algorithmic_bytes": 8.0 * (STEPS + 1) * width[dom] * N_PATHS,
     }
     roofline["hbm"]["frac"] = roofline["hbm"]["achieved_gbs"] / hbm
 
@@ -794,12 +817,14 @@ def run_ours(args, rank, world):
         kms64f = {n: _events(stream, lambda i=i: price_launch(i, _lib.FP64), 2) for i, (n, _) in enumerate(models)}
     ms64f = max_over_ranks(ms64f)
     d64f = max(kms64f, key=kms64f.get)
+    flops_f = FLOPS_PER_PATH_STEP[d64f] * N_PATHS * STEPS
     ops_f = FP64_OPS_PER_PATH_STEP[d64f] * N_PATHS * STEPS
     fp64_fused = {"value": world * path_steps / (ms64f * 1e-3), "unit": "path-steps/s", "ms_per_step": ms64f,
                   "steps": k64f, "kernel_ms": kms64f,
-                  "roofline": {"bound": "fp64 pipe", "kernel": f"k_{d64f}_f64 (fused)",
-                               "achieved": ops_f / (kms64f[d64f] * 1e-3) / 1e9, "peak": peak_fp64_ops / 1e9,
-                               "unit": "G FP64 ops/s", "frac": ops_f / (kms64f[d64f] * 1e-3) / peak_fp64_ops}}
+                  "roofline": {"bound": "fp64 pipe (and issue)", "kernel": f"k_{d64f}_f64 (fused)",
+                               "achieved": flops_f / (kms64f[d64f] * 1e-3) / 1e9, "peak": peak_dfma.value / 1e9,
+                               "unit": "GFLOP/s", "frac": flops_f / (kms64f[d64f] * 1e-3) / peak_dfma.value,
+                               "issued_fp64_pipe_frac": ops_f / (kms64f[d64f] * 1e-3) / peak_fp64_ops}}
     bufs32 = [torch.empty((N_PATHS, STEPS + 1, width[n]) if width[n] > 1 else (N_PATHS, STEPS + 1),
                           dtype=torch.float32, device="cuda") for n, _ in models]
     bytes32 = sum(b.numel() * 4 for b in bufs32)
