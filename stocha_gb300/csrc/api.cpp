@@ -308,6 +308,9 @@ int prepare_model(const stocha_model* m, PathLaunch* L, uint64_t* row_len, u128*
       h.dt = m->t / steps_f;
       h.sqrt_dt = std::sqrt(h.dt);
       h.rho_comp = std::sqrt(1.0 - m->rho * m->rho);
+      h.kdt = m->kappa * h.dt;
+      h.xi_rho = m->xi * m->rho;
+      h.xi_rho_comp = m->xi * h.rho_comp;
       // QE constants (heston.rs:93-94,112-116,143-150): loop-invariant
       // leading subexpressions, evaluated in the reference's order.
       h.e_kdt = std::exp(-m->kappa * h.dt);

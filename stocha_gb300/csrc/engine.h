@@ -25,6 +25,7 @@ struct HestonK {  // heston.rs:45-48 (Euler), :92-97,143-150 (QE)
   double dt, sqrt_dt, rho_comp;
   double e_kdt, k1, qe_m0, qe_s2b, one_m_ekdt;
   double k0_s, k1_s, k2_s, k3_s, k4_s;
+  double kdt, xi_rho, xi_rho_comp;  // kappa dt, xi rho, xi sqrt(1 - rho^2) (FP64 Euler kernel)
   int scheme;  // 0 euler, 1 qe
 };
 struct MertonK {  // jump_diffusion.rs:49-64
