@@ -548,11 +548,11 @@ DRAM_BYTES_PER_ROW = {"multi_gbm": (179.968e3 + 1160.567e6) / 2e5, "heston": (10
 # (DMUL, DADD, DFMA counted once), read from the kernels: the exponential,
 # the sqrt, the conversions and (multi-GBM, Heston) the normals' products run
 # on the integer pipes.
-#   multi-GBM(3): per asset the exponent as a DFMA chain over row i of diffusion*L
-#                 (1 + 2 + 3) and the price product (3 DMUL)
+#   multi-GBM(3): the 3 normals' products (DMUL); per asset the exponent as a DFMA
+#                 chain over row i of diffusion*L (1 + 2 + 3) and the price product (3 DMUL)
 #   Heston Euler: sqrt(v+ dt) 1; xi dW2 2; variance update 3; log increment 2; product 1
 #   Merton: normal product, exponent DFMA, price product (+3 on the ~0.4 % jump steps)
-FP64_OPS_PER_PATH_STEP = {"multi_gbm": 9.0, "heston": 9.0, "merton": 3.0 + 3.0 / 252}
+FP64_OPS_PER_PATH_STEP = {"multi_gbm": 12.0, "heston": 9.0, "merton": 3.0 + 3.0 / 252}
 
 
 def oracle_headline_step(cores):

@@ -152,9 +152,12 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
     }
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
+      // the normals' products by DMUL: with its exponent rows folded (below)
+      // this kernel is bound by issue and the ALU pipe, not by the FP64 pipe
+      // (49 %), so one DMUL is cheaper than the integer-pipe product
 #pragma unroll
-      for (int i = 0; i < na; ++i)  // FP64-pipe bound: integer products
-        z[i] = __longlong_as_double(__double_as_longlong(normal_f64<true>(s, c, zs, err)) ^ zsgn);
+      for (int i = 0; i < na; ++i)
+        z[i] = __longlong_as_double(__double_as_longlong(normal_f64<false>(s, c, zs, err)) ^ zsgn);
 #pragma unroll
       for (int i = 0; i < na; ++i) {
         // exponent drift_i + diffusion_i (L z)_i as one DFMA chain over row i of
