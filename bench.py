@@ -535,10 +535,9 @@ def headline_config(seed=SEED):
 FLOPS_PER_PATH_STEP = {"multi_gbm": 24.0, "heston": 21.0, "merton": 7.0, "gbm": 4.0}
 
 # dram__bytes_read.sum + dram__bytes_write.sum per path row of the materialised
-# FP64 kernels, from ncu captures of 2e5-path launches
-# (profiles/k_multi_gbm_heston_f64_rows_200k.md,
-# profiles/rowstore_paths_materialised_200k.md); the traffic is the written
-# rows, so it scales with the row count.  Dirty data still in L2 when a
+# FP64 kernels, from ncu captures of 2e5-path launches (the ncu summaries of
+# this repository); the traffic is the written rows, so it scales with the
+# row count.  Dirty data still in L2 when a
 # capture ends is not counted, so these sit slightly below the algorithmic
 # 8 * 253 * width bytes a row.
 DRAM_BYTES_PER_ROW = {"multi_gbm": (179.968e3 + 1160.567e6) / 2e5, "heston": (104.960e3 + 351.270e6) / 2e5,
