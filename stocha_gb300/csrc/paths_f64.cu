@@ -343,8 +343,8 @@ __global__ void k_debug_f64(int fn, const double* __restrict__ x, double* __rest
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
     y[i] = fn == 0   ? mul_exp(1.0, x[i], zs)
            : fn == 1 ? sqrt_rn_int(x[i])
-           : fn == 2 ? mul_u53_rn((uint64_t)x[i], zs.xs[i & 255])
-           : fn == 3 ? __dmul_rn(x[i], zs.xs[i & 255])
+           : fn == 2 ? mul_u53_rn((uint64_t)x[i], e64_xs(zs.e64[i & 255]))
+           : fn == 3 ? __dmul_rn(x[i], e64_xs(zs.e64[i & 255]))
                      : mul_exp<false>(1.0, x[i], zs);
 }
 
