@@ -743,16 +743,36 @@ def run_ours(args, rank, world):
         barrier()
         k_e2e = max(1, args.steps // 2) if N_PATHS >= 1_000_000 else args.steps
         t0 = time.perf_counter()
+        marks = [t0]
         for _ in range(k_e2e):
             e2e_step()
-        e2e_s = max_over_ranks((time.perf_counter() - t0) / k_e2e)
+            marks.append(time.perf_counter())
+        e2e_s = max_over_ranks((marks[-1] - t0) / k_e2e)
+        per_step = np.diff(marks) * 1e3
+        # the device-to-host link: 1 GiB from device memory into pinned host memory
+        dsrc = torch.empty(1 << 30, dtype=torch.uint8, device="cuda")
+        hdst = torch.empty(1 << 30, dtype=torch.uint8, pin_memory=True)
+        rates = []
+        for _ in range(5):
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            hdst.copy_(dsrc, non_blocking=True)
+            torch.cuda.synchronize()
+            rates.append((1 << 30) / (time.perf_counter() - t1) / 1e9)
+        link_gbs = float(np.median(rates[1:]))
+        del dsrc, hdst
         e2e = {"value": world * path_steps / e2e_s, "unit": "path-steps/s", "h2d_bytes_per_step": 0,
                "d2h_bytes_per_step": bytes64, "steps": k_e2e, "ms_per_step": e2e_s * 1e3,
+               # rank 0's steps one by one: the link's occasional slow steps
+               # show as max >> median
+               "step_ms": {"median": float(np.median(per_step)), "min": float(per_step.min()),
+                           "max": float(per_step.max())},
+               "link_gbs": link_gbs, "link_floor_ms": bytes64 / (link_gbs * 1e9) * 1e3,
                "first_call_value": world * path_steps / first_s,
                "api": "stocha_gb300.multi_gbm / heston / merton_jump_diffusion -> NumPy float64 arrays",
                "note": "inputs are scalar parameters (kernel arguments); d2h = the three path arrays. The "
-                       "device-to-host link of this box moves 193.6 GB/s by copy engine or SM stores "
-                       "alike (measured), so 10.1 GB take >= 52 ms a step"}
+                       "device-to-host link (link_gbs, measured here with a 1 GiB pinned copy) bounds "
+                       "the step: 10.1 GB take link_floor_ms"}
 
     # ---- FP32 fused pricing (GB300 precision form) ------------------------
     tuning = {}

@@ -493,13 +493,39 @@ static int paths_to_device(stocha_ctx* c, const stocha_model* m, uint64_t seed, 
 }
 
 // Materialised results at least this large overlap their copy with compute
-// when the destination is a cached host buffer: at most 8 row chunks of at
-// least 2^17 rows, about one wave of the FP64 kernels' resident threads (7
-// blocks of 128 per SM on 152 SMs), so each chunk still fills the device and
-// the first copy starts after one wave.  Chunk rows are multiples of 32, so
-// every chunk starts on a whole warp of rows.
+// when the destination is a cached host buffer.  The steady chunk is
+// max(2^17, rows / 8) rows: 2^17 is about one wave of the FP64 kernels'
+// resident threads (7 blocks of 128 per SM on 152 SMs), so a chunk fills the
+// device.  The chunks before it ramp up from 2^14 rows, doubling: a thread
+// computes its whole row, so a full-wave first chunk would hold back the
+// first copy for a whole wave's time (about 1 ms for 3-asset multi-GBM at
+// 252 steps), while 2^14 rows (one warp per scheduler) finish in a fraction
+// of that; each next chunk computes while the one before it copies.
+// Measured on GB300 at 1e6 x 252 FP64 into a cached buffer (median call):
+// multi-GBM 32.73 -> 31.93 ms, Merton 11.02 -> 10.74 ms, Heston 11.57 ->
+// 11.70 ms (a 1.5x ramp, more chunks: 11.78 ms); the link alone takes 31.4
+// and 10.5 ms.  Chunk rows are multiples of 32, so every chunk starts on a
+// whole warp of rows.
 constexpr size_t kOverlapMin = 64u << 20;
-constexpr uint64_t kOverlapMaxChunks = 8, kOverlapMinRows = 1u << 17;
+constexpr uint64_t kOverlapMaxChunks = 8, kOverlapMinRows = 1u << 17, kOverlapFirstRows = 1u << 14;
+constexpr int kOverlapMaxTotal = 32;
+static_assert(sizeof(stocha_ctx::chunk_done) / sizeof(cudaEvent_t) >= kOverlapMaxTotal, "one event per chunk");
+
+// Row boundaries of the overlapped chunks: bound[0] = 0 < ... < bound[n] =
+// rows.  Returns n: at most 9 steady chunks after a ramp of at most 20
+// chunks below 2^36 rows.
+static int overlap_chunks(uint64_t rows, uint64_t bound[kOverlapMaxTotal + 1]) {
+  const uint64_t per = (std::max<uint64_t>(kOverlapMinRows, (rows + kOverlapMaxChunks - 1) / kOverlapMaxChunks) + 31) /
+                       32 * 32;
+  int n = 0;
+  bound[0] = 0;
+  for (uint64_t r = 0, size = kOverlapFirstRows; r < rows && n < kOverlapMaxTotal; ++n) {
+    r = std::min<uint64_t>(rows, r + std::min(size, per));
+    bound[n + 1] = r;
+    if (size < per) size *= 2;
+  }
+  return n;
+}
 
 static int paths_to_host(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, double* out) {
   // Arguments are validated before any CUDA call (as the reference validates
@@ -526,17 +552,15 @@ static int paths_to_host(stocha_ctx* ctx, const stocha_model* m, uint64_t seed, 
       STOCHA_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
       for (cudaEvent_t& e : ctx->chunk_done) STOCHA_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    const uint64_t per = (std::max<uint64_t>(kOverlapMinRows, (m->n_paths + kOverlapMaxChunks - 1) / kOverlapMaxChunks) +
-                          31) / 32 * 32;
-    const uint64_t nch = (m->n_paths + per - 1) / per;
-    for (uint64_t i = 0; i < nch; ++i) {
-      const uint64_t r0 = i * per, r1 = std::min<uint64_t>(m->n_paths, r0 + per);
-      if (r0 < r1 && (rc = paths_to_device(ctx, m, seed, STOCHA_FP64, ctx->out.ptr, r0, r1 - r0))) return rc;
+    uint64_t bound[kOverlapMaxTotal + 1];
+    const int nch = overlap_chunks(m->n_paths, bound);
+    if (bound[nch] != m->n_paths) return set_error(STOCHA_ERR_VALUE, "too many rows for the overlapped copy");
+    for (int i = 0; i < nch; ++i) {
+      if ((rc = paths_to_device(ctx, m, seed, STOCHA_FP64, ctx->out.ptr, bound[i], bound[i + 1] - bound[i]))) return rc;
       STOCHA_CUDA(cudaEventRecord(ctx->chunk_done[i], ctx->stream));
     }
-    for (uint64_t i = 0; i < nch; ++i) {
-      const uint64_t r0 = i * per, r1 = std::min<uint64_t>(m->n_paths, r0 + per);
-      if (r0 >= r1) break;
+    for (int i = 0; i < nch; ++i) {
+      const uint64_t r0 = bound[i], r1 = bound[i + 1];
       STOCHA_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_done[i], 0));
       const size_t o = (size_t)r0 * row_len, n = (size_t)(r1 - r0) * row_len;
       STOCHA_CUDA(cudaMemcpyAsync(out + o, (const double*)ctx->out.ptr + o, n * sizeof(double), cudaMemcpyDeviceToHost,

@@ -48,7 +48,7 @@ struct stocha_ctx {
   stocha::LsmcGraphs* lsmc_graphs = nullptr;  // LSMC sweep graphs for this context's stream
   // overlap of materialised results' device-to-host copies with their compute
   cudaStream_t copy_stream = nullptr;
-  cudaEvent_t chunk_done[8] = {};
+  cudaEvent_t chunk_done[32] = {};
   std::recursive_mutex mu;
 };
 

@@ -58,11 +58,24 @@ def test_multi_gbm_row_layouts(stocha, oracle, na, steps):
     assert _rel(got, want) <= PATH_RTOL
 
 
+def _overlap_bounds(rows):
+    """Row boundaries of the overlapped copy's chunks: a ramp from 2^14 rows,
+    doubling, up to the steady max(2^17, rows / 8) rows (rounded up to 32)."""
+    per = (max(1 << 17, (rows + 7) // 8) + 31) // 32 * 32
+    b, size = [0], 1 << 14
+    while b[-1] < rows:
+        b.append(min(rows, b[-1] + min(size, per)))
+        size = size * 2 if size < per else size
+    return b
+
+
 def test_chunked_host_copy(stocha, oracle):
     """2^21 + 8 rows of 9 doubles into a cached host buffer: the overlap path
-    computes 8 row chunks (multiples of 32 rows) whose copies overlap the
-    next chunk.  The result must equal the one-launch result (first call,
-    fresh memory) and the oracle around every chunk boundary."""
+    computes row chunks (a ramp of 2^14, 2^15, ... 2^18 rows, then
+    262 176-row chunks; all multiples of 32 rows) whose copies overlap the
+    next chunk.
+    The result must equal the one-launch result (first call, fresh memory)
+    and the oracle around every chunk boundary."""
     n, steps = (1 << 21) + 8, 8
     kw = dict(s0=100.0, mu=0.05, sigma=0.2, t=1.0, steps=steps, n_paths=n, seed=21)
     a = stocha.gbm(**kw)
@@ -72,11 +85,11 @@ def test_chunked_host_copy(stocha, oracle):
     gc.collect()
     b = stocha.gbm(**kw)  # the cached buffer: chunked launches
     np.testing.assert_array_equal(b, first)
-    per = ((n + 7) // 8 + 31) // 32 * 32
-    k = 7 * per + 40
-    want = oracle.gbm(100.0, 0.05, 0.2, 1.0, steps, k, seed=21, threads=8)
-    for c in range(1, 8):
-        lo, hi = c * per - 40, c * per + 40
+    bounds = _overlap_bounds(n)[1:-1]
+    assert bounds[:5] == [1 << 14, 3 << 14, 7 << 14, 15 << 14, 31 << 14] and len(bounds) == 11
+    want = oracle.gbm(100.0, 0.05, 0.2, 1.0, steps, bounds[-1] + 40, seed=21, threads=8)
+    for c in bounds:
+        lo, hi = c - 40, c + 40
         assert _rel(b[lo:hi], want[lo:hi]) <= PATH_RTOL, c
 
 
