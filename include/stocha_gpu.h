@@ -110,7 +110,10 @@ int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n);
  * number: 0 exp (as stocha_debug_exp), 1 sqrt (as stocha_debug_sqrt), 2 the
  * normal's product (uint64)x[i] * X[L] 2^-53 with L = i mod 256 on the integer
  * pipes, 3 the same product by the FP64 pipe (they must agree bit for bit),
- * 4 exp in the early-exit form (bit for bit the same as 0). */
+ * 4 exp in the early-exit form (bit for bit the same as 0), 5 the path
+ * kernels' ziggurat tail value -ln(u1)/R + R for the draw whose 64 bits are
+ * those of x[i] (u1 = (draw >> 11) 2^-53, draw >> 11 >= 1), 6 the same value
+ * as the RNG's normals compute it (FP64 log and division). */
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n);
 /* Diagnostic (no counterpart in the reference): the error of the device's
  * hardware logarithm __logf over every normal float x in (0, 1), against

@@ -69,6 +69,7 @@ void build_tables(ZigTables* t) {
   t->r = STOCHA_ZIG_R_HEX;
   t->r32 = (float)t->r;
   t->nrinv32 = (float)(-1.0 / t->r);
+  t->nrinv = -1.0 / t->r;
   static const uint64_t E2[256] = STOCHA_EXP2_Q63_INIT;
   for (int j = 0; j < 256; ++j) t->exp2q[j] = E2[j];
 }
@@ -825,7 +826,7 @@ int stocha_debug_exp(stocha_ctx* ctx, const double* x, double* y, uint64_t n) { 
 int stocha_debug_sqrt(stocha_ctx* ctx, const double* x, double* y, uint64_t n) { return debug_f64(1, ctx, x, y, n); }
 
 int stocha_debug_f64(stocha_ctx* ctx, int32_t fn, const double* x, double* y, uint64_t n) {
-  if (fn < 0 || fn > 4) return set_error(STOCHA_ERR_VALUE, "fn must be 0..4");
+  if (fn < 0 || fn > 6) return set_error(STOCHA_ERR_VALUE, "fn must be 0..6");
   return debug_f64(fn, ctx, x, y, n);
 }
 

@@ -38,6 +38,7 @@ struct ZigTables {
   double r;
   float r32;
   float nrinv32;  // -1/R rounded to float (the FP32 tail test's x = ln(u1) * nrinv32)
+  double nrinv;   // -1/R (the path kernels' FP64 tail value)
   uint64_t exp2q[256];  // 2^(j/256) * 2^63 (integer-pipe exponential)
 };
 

@@ -101,8 +101,8 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
     uint64_t k = 1;
 #pragma unroll 1
     for (; k + 1 <= a.steps; k += 2) {
-      const double z0 = normal_f64(s, c, zs, err);
-      const double z1 = normal_f64(s, c, zs, err);
+      const double z0 = normal_f64<false, true>(s, c, zs, err);
+      const double z1 = normal_f64<false, true>(s, c, zs, err);
       const double y0 = exp_y(fma(diffusion, z0, drift), zs);
       const double y1 = exp_y(fma(diffusion, z1, drift), zs);
       x *= y0;
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(128) k_gbm_f64(const __grid_constant__ PathLau
       if (kStore) emit64(out, a, lrow, k + 1, 1, 0, x);
     }
     if (k <= a.steps) {
-      const double z = normal_f64(s, c, zs, err);
+      const double z = normal_f64<false, true>(s, c, zs, err);
       x = mul_exp(x, fma(diffusion, z, drift), zs);
       if (kStore) emit64(out, a, lrow, k, 1, 0, x);
     }
@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(128) k_multi_gbm_f64(const __grid_constant__ P
       // (49 %), so one DMUL is cheaper than the integer-pipe product
 #pragma unroll
       for (int i = 0; i < na; ++i)
-        z[i] = __longlong_as_double(__double_as_longlong(normal_f64<false>(s, c, zs, err)) ^ zsgn);
+        z[i] = __longlong_as_double(__double_as_longlong(normal_f64<false, true>(s, c, zs, err)) ^ zsgn);
 #pragma unroll
       for (int i = 0; i < na; ++i) {
         // exponent drift_i + diffusion_i (L z)_i as one DFMA chain over row i of
@@ -207,8 +207,8 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
       const double mu_dt = h.mu * h.dt, nhalf_dt = -0.5 * h.dt;
 #pragma unroll 1
       for (uint64_t k = 1; k <= a.steps; ++k) {
-        const double dw1 = normal_f64<true>(s, c, zs, err);  // FP64-pipe bound: integer products
-        const double dz = normal_f64<true>(s, c, zs, err);
+        const double dw1 = normal_f64<true, true>(s, c, zs, err);  // FP64-pipe bound: integer products
+        const double dz = normal_f64<true, true>(s, c, zs, err);
         const double v_plus = max0_int(v);
         // w = sqrt(v+ dt) serves both updates; sqrt(v+) is the correctly
         // rounded one, on the integer pipes
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
           b2 = fmax(b2, 0.0);
           double aa = m / (1.0 + b2);
           double b = sqrt(b2);
-          double z = normal_f64(s, c, zs, err);
+          double z = normal_f64<false, true>(s, c, zs, err);
           v_next = aa * (b + z) * (b + z);
         } else {
           double p = (psi - 1.0) / (psi + 1.0);
@@ -249,7 +249,7 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
           v_next = (u <= p) ? 0.0 : log((1.0 - p) / (1.0 - u)) / beta;
         }
         v_next = fmax(v_next, 0.0);
-        double z1 = normal_f64(s, c, zs, err);
+        double z1 = normal_f64<false, true>(s, c, zs, err);
         double var_term = fmax(h.k3_s * v_plus + h.k4_s * v_next, 0.0);
         double log_s = log(x) + h.k0_s + h.k1_s * v_plus + h.k2_s * v_next + sqrt(var_term) * z1;
         x = exp(fmin(fmax(log_s, -500.0), 500.0));
@@ -267,8 +267,10 @@ __global__ void __launch_bounds__(128) k_heston_f64(const __grid_constant__ Path
   if (err) atomicOr(a.err, err);
 }
 
+// 9 resident blocks in the store modes (56 registers): 2.856 -> 2.815 ms at
+// 1e6 x 252 materialised on GB300 (the same cap made multi-GBM slower).
 template <int kMode>
-__global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ PathLaunch a) {
+__global__ void __launch_bounds__(128, kMode == kFused ? 1 : 9) k_merton_f64(const __grid_constant__ PathLaunch a) {
   constexpr bool kStore = kMode != kFused;
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, true);
@@ -286,11 +288,11 @@ __global__ void __launch_bounds__(128) k_merton_f64(const __grid_constant__ Path
     if (kStore) emit64(out, a, lrow, 0, 1, 0, x);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
-      const double z = normal_f64(s, c, zs, err);
+      const double z = normal_f64<false, true>(s, c, zs, err);
       double ret = fma(M.diffusion, z, M.drift);
       const uint64_t u = s.next();
       if ((u >> 11) < M.jump_thr) {  // the reference adds a zero jump return otherwise
-        const double z_j = normal_f64(s, c, zs, err);
+        const double z_j = normal_f64<false, true>(s, c, zs, err);
         ret += fma(M.sigma_j, z_j, M.mu_j);
       }
       x = mul_exp<false>(x, ret, zs);  // issue-bound: the early-exit form
@@ -325,7 +327,8 @@ __global__ void __launch_bounds__(128) k_hull_white_f64(const __grid_constant__ 
     emit64(out, a, lrow, 0, 1, 0, x);
 #pragma unroll 1
     for (uint64_t k = 1; k <= a.steps; ++k) {
-      const double z = normal_f64(s, c, zs, err);
+      // the exact tail value: the rate paths are bit-exact with the reference
+      const double z = normal_f64<false, false>(s, c, zs, err);
       x = x * H.e + H.mean_reversion + H.vol * z;
       emit64(out, a, lrow, k, 1, 0, x);
     }
@@ -345,6 +348,8 @@ __global__ void k_debug_f64(int fn, const double* __restrict__ x, double* __rest
            : fn == 1 ? sqrt_rn_int(x[i])
            : fn == 2 ? mul_u53_rn((uint64_t)x[i], e64_xs(zs.e64[i & 255]))
            : fn == 3 ? __dmul_rn(x[i], e64_xs(zs.e64[i & 255]))
+           : fn == 5 ? tail_value_fast_f64((uint64_t)__double_as_longlong(x[i]), tabs, zs)
+           : fn == 6 ? tail_value_f64((uint64_t)__double_as_longlong(x[i]), tabs->r)
                      : mul_exp<false>(1.0, x[i], zs);
 }
 

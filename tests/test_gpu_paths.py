@@ -273,6 +273,33 @@ def test_integer_normal_product_equals_dmul(stocha):
     assert (y_fp[:256] == 0).all() and (y_fp[256:] >= 0).all()
 
 
+def test_fast_tail_value_error(stocha):
+    """The path kernels' tail value (hardware logarithm + one Newton step
+    through the integer-pipe exponential, 8 FP64 operations) against the FP64
+    log-and-divide form the RNG's normals use: within 1e-15 relative over 1e6
+    random draws and the extremes of u1 = (draw >> 11) 2^-53 (the smallest
+    draws, ln u1 = -36.7, take exp's |t| >= 16 branch)."""
+    import ctypes
+
+    from stocha_gb300 import _lib
+    lib = _lib.load()
+    P = ctypes.POINTER(ctypes.c_double)
+    rng = np.random.default_rng(77)
+    m = rng.integers(1, 1 << 53, size=1_000_000, dtype=np.uint64)
+    edge = np.array([1, 2, 3, 1000, 1 << 20, 1 << 30, (1 << 36) + 7, 1 << 52, (1 << 52) - 1, (1 << 52) + 1,
+                     (1 << 53) - 1, (1 << 53) - 2, int(0.999999 * 2 ** 53), int(0.5 * 2 ** 53)], dtype=np.uint64)
+    m = np.concatenate([m, edge])
+    draws = (m << np.uint64(11)) | rng.integers(0, 1 << 11, size=m.size, dtype=np.uint64)
+    x = draws.view(np.float64)
+    fast = np.empty_like(x)
+    exact = np.empty_like(x)
+    _lib.check(lib.stocha_debug_f64(None, 5, x.ctypes.data_as(P), fast.ctypes.data_as(P), x.size))
+    _lib.check(lib.stocha_debug_f64(None, 6, x.ctypes.data_as(P), exact.ctypes.data_as(P), x.size))
+    assert np.isfinite(fast).all() and (exact >= 3.6).all()
+    rel = np.abs(fast - exact) / exact
+    assert rel.max() <= 1e-15, (rel.max(), m[rel.argmax()])
+
+
 def test_fast_log_error_bounds(stocha):
     """The ziggurat tail test decides in FP32 with the hardware logarithm
     (__logf) and falls back to FP64 within a margin built from its error
