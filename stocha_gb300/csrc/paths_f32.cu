@@ -129,28 +129,24 @@ __device__ __forceinline__ void run_rows(const PathLaunch& a, Batch&& batch) {
       if (lane == 0) base = atomicAdd(a.work, (unsigned long long)a.batch_rows);
       base = __shfl_sync(0xFFFFFFFFu, base, 0);
       if (base >= a.rows) break;
-      Kahan s[NV], s2[NV];
+      double* rec = a.partials + (base / a.batch_rows) * (2 * NV);
+      // Each group of 32 rows is added into the record at once (FP64 warp
+      // tree, then lane 0 adds it to the record in group order), so no sum
+      // stays live in registers while the next row is simulated.
 #pragma unroll 1
       for (uint32_t j = 0; j < per_lane; ++j) {
         const uint64_t b = base + 32ull * j;
         if (b >= a.rows) break;  // warp-uniform
         float p[NV];
-        if (batch(b, p)) {
+        const bool ok = batch(b, p);
 #pragma unroll
-          for (int i = 0; i < NV; ++i) {
-            s[i].add(p[i]);
-            s2[i].add(p[i] * p[i]);
+        for (int i = 0; i < NV; ++i) {
+          const double v = warp_sum(ok ? (double)p[i] : 0.0);
+          const double v2 = warp_sum(ok ? (double)(p[i] * p[i]) : 0.0);
+          if (lane == 0) {
+            rec[2 * i] = j ? rec[2 * i] + v : v;
+            rec[2 * i + 1] = j ? rec[2 * i + 1] + v2 : v2;
           }
-        }
-      }
-      double* rec = a.partials + (base / a.batch_rows) * (2 * NV);
-#pragma unroll
-      for (int i = 0; i < NV; ++i) {
-        const double v = warp_sum((double)s[i].value());
-        const double v2 = warp_sum((double)s2[i].value());
-        if (lane == 0) {
-          rec[2 * i] = v;
-          rec[2 * i + 1] = v2;
         }
       }
     }
@@ -685,9 +681,12 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_multi_f
 
 // Rows of one warp: base (warp-uniform) + lane.  A lane past the end runs on
 // the first row's stream and contributes nothing.
+// The kernels draw with pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi): the stream
+// increment is read from the launch parameters at every draw (it stays in the
+// constant bank instead of four registers of every lane).
 struct WarpRow {
   bool ok, neg;
-  PcgGen s;
+  DevPcg st;
 };
 
 __device__ __forceinline__ WarpRow warp_row(const PathLaunch& a, uint64_t base) {
@@ -696,7 +695,7 @@ __device__ __forceinline__ WarpRow warp_row(const PathLaunch& a, uint64_t base) 
   r.ok = lrow < a.rows;
   const uint64_t row = a.row_begin + (r.ok ? lrow : base);
   r.neg = row >= a.base_paths;
-  r.s = PcgGen{pcg_path_state(a.ss, r.neg ? row - a.base_paths : row), a.ss.inc_lo, a.ss.inc_hi};
+  r.st = pcg_path_state(a.ss, r.neg ? row - a.base_paths : row);
   return r;
 }
 
@@ -706,8 +705,9 @@ __device__ __forceinline__ WarpRow warp_row(const PathLaunch& a, uint64_t base) 
 __device__ __forceinline__ uint32_t uf_cap(uint32_t normals) { return 64 * normals + 4096; }
 
 // Calls feed() (one draw per lane) in groups of kUfUnroll until every lane's
-// count has reached its need; the warp vote runs once per group.
-constexpr int kUfUnroll = 4;
+// count has reached its need; the warp vote runs once per group (8 draws a
+// group: measured on GB300 with ZigFeed, 3-asset sums 1.79 -> 1.71 ms over 4).
+constexpr int kUfUnroll = 8;
 template <class F>
 __device__ __forceinline__ void uf_drive(const uint32_t& cnt, uint32_t need, uint32_t cap, unsigned& err, F&& feed) {
   uint32_t it = 0;
@@ -729,8 +729,8 @@ __device__ __forceinline__ void uf_drive(const uint32_t& cnt, uint32_t need, uin
 template <int NA>
 __global__ void __launch_bounds__(256, kUfMinBlocks) k_gbm_uf(const __grid_constant__ PathLaunch a) {
   constexpr int N = NA > 0 ? NA : 1;
-  __shared__ ZigShared zs;
-  zig_stage(zs, a.tabs, false);
+  __shared__ ZigShared32 zs;
+  zig_stage32(zs, a.tabs);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const F32K& f = a.f32;
   unsigned err = 0;
@@ -738,12 +738,12 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_gbm_uf(const __grid_const
   run_rows<N>(a, [&](uint64_t base, float* pay) {
     WarpRow r = warp_row(a, base);
     Plain w[N];
-    ZigLane q;
+    ZigFeed q;
     const uint32_t need = r.ok ? need_all : 0;
     uint32_t cnt = 0;
     uf_drive(cnt, need, cap, err, [&]() {
       float z;
-      if (zig_feed(q, r.s.next(), c, zs, z) && cnt < need) {
+      if (q.feed(pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z) & (cnt < need)) {
         w[0].add(z);  // the antithetic sign is applied to the sums
         ++cnt;
         if constexpr (N > 1) {
@@ -779,9 +779,9 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_gbm_uf(const __grid_const
 }
 
 // Heston (Euler): normals pair up as (dw1, dz) of one step.
-__global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathLaunch a) {
-  __shared__ ZigShared zs;
-  zig_stage(zs, a.tabs, false);
+__global__ void __launch_bounds__(256, kUfMinBlocks) k_heston_uf(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared32 zs;
+  zig_stage32(zs, a.tabs);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const F32K& f = a.f32;
   const float rho = f.h_rho, rho_comp = f.h_rho_comp, kappa_dt = f.h_kdt, theta = f.h_theta;
@@ -790,7 +790,7 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
   const uint32_t cap = uf_cap(2 * (uint32_t)a.steps);
   run_rows<1>(a, [&](uint64_t base, float* pay) {
     WarpRow r = warp_row(a, base);
-    ZigLane q;
+    ZigFeed q;
     Plain lg;
     float v = f.h_v0, dw1 = 0.0f;
     bool half = false;
@@ -798,7 +798,7 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
     uint32_t cnt = 0;
     uf_drive(cnt, need, cap, err, [&]() {
       float z;
-      if (zig_feed(q, r.s.next(), c, zs, z) && cnt < need) {
+      if (q.feed(pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z) & (cnt < need)) {
         if (!half) {
           dw1 = z;
           half = true;
@@ -822,9 +822,9 @@ __global__ void __launch_bounds__(256) k_heston_uf(const __grid_constant__ PathL
 // Merton: after the diffusion normal of a step the lane takes the jump
 // uniform at once (a second generator step in the same iteration); on a jump
 // its next normal is the jump size.
-__global__ void __launch_bounds__(256, kFusedMinBlocks) k_merton_uf(const __grid_constant__ PathLaunch a) {
-  __shared__ ZigShared zs;
-  zig_stage(zs, a.tabs, false);
+__global__ void __launch_bounds__(256, kUfMinBlocks) k_merton_uf(const __grid_constant__ PathLaunch a) {
+  __shared__ ZigShared32 zs;
+  zig_stage32(zs, a.tabs);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
   const F32K& f = a.f32;
   const float mu_j = f.m_mu_j, sigma_j = f.m_sigma_j;
@@ -833,7 +833,7 @@ __global__ void __launch_bounds__(256, kFusedMinBlocks) k_merton_uf(const __grid
   const uint32_t cap = uf_cap(2 * (uint32_t)a.steps);
   run_rows<1>(a, [&](uint64_t base, float* pay) {
     WarpRow r = warp_row(a, base);
-    ZigLane q;
+    ZigFeed q;
     Plain w;
     float jumps = 0.0f;
     bool in_jump = false;
@@ -841,14 +841,14 @@ __global__ void __launch_bounds__(256, kFusedMinBlocks) k_merton_uf(const __grid
     uint32_t cnt = 0;
     uf_drive(cnt, need, cap, err, [&]() {
       float z;
-      if (zig_feed(q, r.s.next(), c, zs, z) && cnt < need) {
+      if (q.feed(pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z) & (cnt < need)) {
         if (in_jump) {
           jumps += fmaf(sigma_j, z, mu_j);
           in_jump = false;
           ++cnt;
         } else {
           w.add(z);
-          if ((r.s.next() >> 11) < thr)
+          if ((pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi) >> 11) < thr)
             in_jump = true;
           else
             ++cnt;
