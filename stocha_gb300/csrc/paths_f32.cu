@@ -708,7 +708,7 @@ __device__ __forceinline__ uint32_t uf_cap(uint32_t normals) { return 64 * norma
 // count has reached its need; the warp vote runs once per group (8 draws a
 // group: measured on GB300 with ZigFeed, 3-asset sums 1.79 -> 1.71 ms over 4).
 constexpr int kUfUnroll = 8;
-template <class F>
+template <int kU = kUfUnroll, class F>
 __device__ __forceinline__ void uf_drive(const uint32_t& cnt, uint32_t need, uint32_t cap, unsigned& err, F&& feed) {
   uint32_t it = 0;
 #pragma unroll 1
@@ -718,8 +718,8 @@ __device__ __forceinline__ void uf_drive(const uint32_t& cnt, uint32_t need, uin
       break;
     }
 #pragma unroll
-    for (int j = 0; j < kUfUnroll; ++j) feed();
-    it += kUfUnroll;
+    for (int j = 0; j < kU; ++j) feed();
+    it += kU;
   }
 }
 
@@ -778,7 +778,13 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_gbm_uf(const __grid_const
   if (err) atomicOr(a.err, err);
 }
 
-// Heston (Euler): normals pair up as (dw1, dz) of one step.
+// Heston (Euler): normals pair up as (dw1, dz) of one step.  Each call feeds
+// two draws, and at most one step completes per call: the lane's phase (half:
+// a dw1 is carried from an earlier call) picks the step's two normals from
+// the carried one and this call's.  Lanes drift out of phase after rejected
+// attempts; with one draw a call the step's arithmetic issued for the warp in
+// almost every call (85 warp instructions a draw on GB300), with two it issues
+// once per two draws.
 __global__ void __launch_bounds__(256, kUfMinBlocks) k_heston_uf(const __grid_constant__ PathLaunch a) {
   __shared__ ZigShared32 zs;
   zig_stage32(zs, a.tabs);
@@ -792,25 +798,32 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_heston_uf(const __grid_co
     WarpRow r = warp_row(a, base);
     ZigFeed q;
     Plain lg;
-    float v = f.h_v0, dw1 = 0.0f;
+    float v = f.h_v0, zc = 0.0f;
     bool half = false;
     const uint32_t need = r.ok ? (uint32_t)a.steps : 0;
     uint32_t cnt = 0;
-    uf_drive(cnt, need, cap, err, [&]() {
-      float z;
-      if (q.feed(pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z) & (cnt < need)) {
-        if (!half) {
-          dw1 = z;
-          half = true;
-        } else {
-          const float dw2 = fmaf(rho, dw1, rho_comp * z);
-          const float v_plus = fmaxf(v, 0.0f);
-          const float sqrt_v = sqrt_approx(v_plus);
-          v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
-          lg.add(fmaf(nhdt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
-          half = false;
-          ++cnt;
-        }
+    uf_drive<kUfUnroll / 2>(cnt, need, cap, err, [&]() {
+      float z1, z2;
+      const bool a1 = q.feed(pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z1);
+      const bool a2 = q.feed(pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z2);
+      const float first = a1 ? z1 : z2;
+      const bool two = a1 & a2, one = a1 ^ a2;
+      const bool step = half ? (a1 | a2) : two;
+      const float dw1 = half ? zc : z1;
+      const float dz = half ? first : z2;
+      if (half) {
+        if (two) zc = z2;
+      } else if (one) {
+        zc = first;
+      }
+      half ^= one;
+      if (step & (cnt < need)) {
+        const float dw2 = fmaf(rho, dw1, rho_comp * dz);
+        const float v_plus = fmaxf(v, 0.0f);
+        const float sqrt_v = sqrt_approx(v_plus);
+        v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
+        lg.add(fmaf(nhdt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
+        ++cnt;
       }
     });
     if (r.ok) pay[0] = payoff_f32(f.h_s0 * expf(lg.value()), f.strike, a.payoff);
