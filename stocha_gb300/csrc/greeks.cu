@@ -98,15 +98,32 @@ __device__ __forceinline__ void contribute(const GInst& I, float S, float S_sp, 
   acc[8].add(pay(sm, I.K, call));
 }
 
+// The paths of a warp are 32 consecutive ones (base + lane), simulated with
+// the warp-uniform sampler feed (ZigFeed): every lane steps its generator in
+// the same instruction each iteration and only wedge tests and the tail
+// diverge.  Draws and FP32 values are those of normal_f32 one normal after
+// another, and every per-path sum adds them in the same order, so the results
+// are those of a per-thread loop over normal_f32.  A lane past the chunk end
+// (ok false) runs on a valid stream and contributes nothing.
 template <bool PO>
-__device__ void path_gbm(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
-                         K32* acc) {
-  PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
+__device__ void path_gbm(const GInst& I, uint64_t p, bool ok, const SamplerCtx& c, const ZigShared32& zs,
+                         unsigned& err, K32* acc) {
+  DevPcg st = pcg_path_state(I.ss, p);
+  ZigFeed q;
   // plain FP32 sum of the normals: every scenario of the path is a closed
   // form of the same W, so its rounding (~5e-6 over 252 steps) moves them
   // together and cancels in the bump differences
   float W = 0.0f;
-  for (uint64_t k = 0; k < I.steps; ++k) W += normal_f32(g, c, zs, err);
+  const uint32_t need = ok ? (uint32_t)I.steps : 0u;
+  uint32_t cnt = 0;
+  uf_drive(cnt, need, uf_cap(I.steps), err, [&]() {
+    float z;
+    if (q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z) & (cnt < need)) {
+      W += z;
+      ++cnt;
+    }
+  });
+  if (!ok) return;
   constexpr int NT = PO ? 1 : 4;
   float S[4];
 #pragma unroll
@@ -114,26 +131,46 @@ __device__ void path_gbm(const GInst& I, uint64_t p, const SamplerCtx& c, const 
   contribute<PO>(I, S[0], S[PO ? 0 : 1], S[PO ? 0 : 2], S[PO ? 0 : 3], acc);
 }
 
-__device__ void merton_pass(const GInst& I, uint64_t p, uint64_t thr, const SamplerCtx& c, const ZigShared& zs,
-                            unsigned& err, float* W, float* J) {
-  PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
+// Merton: after the diffusion normal of a step the lane takes the jump
+// uniform at once (a second generator step in the same iteration); on a jump
+// its next normal is the jump size.
+__device__ void merton_pass(const GInst& I, uint64_t p, bool ok, uint64_t thr, const SamplerCtx& c,
+                            const ZigShared32& zs, unsigned& err, float* W, float* J) {
+  DevPcg st = pcg_path_state(I.ss, p);
+  ZigFeed q;
   float w = 0.0f;  // plain sum, as for GBM
   float jumps = 0.0f;
-  for (uint64_t k = 0; k < I.steps; ++k) {
-    w += normal_f32(g, c, zs, err);
-    if ((g.next() >> 11) < thr) jumps += fmaf(I.sigma_j, normal_f32(g, c, zs, err), I.mu_j);
-  }
+  bool in_jump = false;
+  const uint32_t need = ok ? (uint32_t)I.steps : 0u;
+  uint32_t cnt = 0;
+  uf_drive(cnt, need, uf_cap(2 * I.steps), err, [&]() {
+    float z;
+    if (q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z) & (cnt < need)) {
+      if (in_jump) {
+        jumps += fmaf(I.sigma_j, z, I.mu_j);
+        in_jump = false;
+        ++cnt;
+      } else {
+        w += z;
+        if ((pcg_next(st, I.ss.inc_lo, I.ss.inc_hi) >> 11) < thr)
+          in_jump = true;
+        else
+          ++cnt;
+      }
+    }
+  });
   *W = w;
   *J = jumps;
 }
 
 template <bool PO>
-__device__ void path_merton(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
-                            K32* acc) {
+__device__ void path_merton(const GInst& I, uint64_t p, bool ok, const SamplerCtx& c, const ZigShared32& zs,
+                            unsigned& err, K32* acc) {
   float W, J;
-  merton_pass(I, p, I.jthr[0], c, zs, err, &W, &J);
+  merton_pass(I, p, ok, I.jthr[0], c, zs, err, &W, &J);
   float S[4];
   if constexpr (PO) {
+    if (!ok) return;
     S[0] = I.s0 * expf(fmaf(I.diff[0], W, I.kdrift[0]) + J);
     contribute<true>(I, S[0], S[0], S[0], S[0], acc);
   } else {
@@ -141,20 +178,25 @@ __device__ void path_merton(const GInst& I, uint64_t p, const SamplerCtx& c, con
     for (int t = 0; t < 3; ++t) S[t] = I.s0 * expf(fmaf(I.diff[t], W, I.kdrift[t]) + J);
     if (I.theta_pass) {
       float W2, J2;
-      merton_pass(I, p, I.jthr[1], c, zs, err, &W2, &J2);
+      merton_pass(I, p, ok, I.jthr[1], c, zs, err, &W2, &J2);
       S[3] = I.s0 * expf(fmaf(I.diff[3], W2, I.kdrift[3]) + J2);
     } else {
       S[3] = S[0];
     }
+    if (!ok) return;
     contribute<false>(I, S[0], S[1], S[2], S[3], acc);
   }
 }
 
+// Heston: two draws a call and at most one step a call, its normals picked by
+// the lane's phase (as in the fused pricing kernel): the steps' arithmetic,
+// four scenarios of it for the Greeks, issues once per two draws.
 template <bool PO>
-__device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, const ZigShared& zs, unsigned& err,
-                            K32* acc) {
+__device__ void path_heston(const GInst& I, uint64_t p, bool ok, const SamplerCtx& c, const ZigShared32& zs,
+                            unsigned& err, K32* acc) {
   constexpr int NT = PO ? 1 : 4;
-  PcgGen g{pcg_path_state(I.ss, p), I.ss.inc_lo, I.ss.inc_hi};
+  DevPcg st = pcg_path_state(I.ss, p);
+  ZigFeed q;
   float v[4];
   K32 lg[4];
 #pragma unroll
@@ -162,18 +204,38 @@ __device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, con
     v[t] = I.hv0[t];
     lg[t] = K32{0.0f, 0.0f};
   }
-  for (uint64_t k = 0; k < I.steps; ++k) {
-    const float dw1 = normal_f32(g, c, zs, err);
-    const float dz = normal_f32(g, c, zs, err);
-    const float dw2 = fmaf(I.hrho, dw1, I.hrho_comp * dz);
-#pragma unroll
-    for (int t = 0; t < NT; ++t) {
-      const float vp = fmaxf(v[t], 0.0f);
-      const float sv = sqrt_approx(vp);
-      v[t] += fmaf(I.hkdt[t], I.htheta - vp, I.hxsdt[t] * sv * dw2);
-      lg[t].add(fmaf(I.hnhdt[t], vp, I.hmudt[t]) + sv * I.hsdt[t] * dw1);
+  float zc = 0.0f;
+  bool half = false;
+  const uint32_t need = ok ? (uint32_t)I.steps : 0u;
+  uint32_t cnt = 0;
+  uf_drive<kUfUnroll / 2>(cnt, need, uf_cap(2 * I.steps), err, [&]() {
+    float z1, z2;
+    const bool a1 = q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z1);
+    const bool a2 = q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z2);
+    const float first = a1 ? z1 : z2;
+    const bool two = a1 & a2, one = a1 ^ a2;
+    const bool step = half ? (a1 | a2) : two;
+    const float dw1 = half ? zc : z1;
+    const float dz = half ? first : z2;
+    if (half) {
+      if (two) zc = z2;
+    } else if (one) {
+      zc = first;
     }
-  }
+    half ^= one;
+    if (step & (cnt < need)) {
+      const float dw2 = fmaf(I.hrho, dw1, I.hrho_comp * dz);
+#pragma unroll
+      for (int t = 0; t < NT; ++t) {
+        const float vp = fmaxf(v[t], 0.0f);
+        const float sv = sqrt_approx(vp);
+        v[t] += fmaf(I.hkdt[t], I.htheta - vp, I.hxsdt[t] * sv * dw2);
+        lg[t].add(fmaf(I.hnhdt[t], vp, I.hmudt[t]) + sv * I.hsdt[t] * dw1);
+      }
+      ++cnt;
+    }
+  });
+  if (!ok) return;
   float S[4];
 #pragma unroll
   for (int t = 0; t < NT; ++t) S[t] = I.s0 * expf(lg[t].s - lg[t].c);
@@ -184,18 +246,22 @@ __device__ void path_heston(const GInst& I, uint64_t p, const SamplerCtx& c, con
 // block totals (compensated FP32 per thread and per warp, FP64 across warps).
 template <bool PO>
 __device__ __forceinline__ void run_item(const GInst& I, uint64_t lo, uint64_t hi, const SamplerCtx& c,
-                                         const ZigShared& zs, unsigned& err, double* out) {
+                                         const ZigShared32& zs, unsigned& err, double* out) {
   constexpr int NA = PO ? 2 : kGreekAcc;
   K32 acc[kGreekAcc];
 #pragma unroll
   for (int j = 0; j < kGreekAcc; ++j) acc[j] = K32{0.0f, 0.0f};
-  for (uint64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+  // warp-uniform loop: the sampler feed votes across all 32 lanes
+  for (uint64_t b = lo + (threadIdx.x & ~31u); b < hi; b += blockDim.x) {
+    const uint64_t p = b + (threadIdx.x & 31u);
+    const bool ok = p < hi;
+    const uint64_t pp = ok ? p : b;
     if (I.model == kGbm)
-      path_gbm<PO>(I, p, c, zs, err, acc);
+      path_gbm<PO>(I, pp, ok, c, zs, err, acc);
     else if (I.model == kHeston)
-      path_heston<PO>(I, p, c, zs, err, acc);
+      path_heston<PO>(I, pp, ok, c, zs, err, acc);
     else
-      path_merton<PO>(I, p, c, zs, err, acc);
+      path_merton<PO>(I, pp, ok, c, zs, err, acc);
   }
   float s[NA], cc[NA];
 #pragma unroll
@@ -229,9 +295,9 @@ __device__ __forceinline__ uint32_t inst_of_item(const GreeksLaunch& g, unsigned
 // issue-bound like the fused pricing kernels, and the extra warps hide more
 // of the generator's latency (512-instance batch 90 -> 84 ms on GB300).
 __global__ void __launch_bounds__(256, 3) k_greeks(const GreeksLaunch g) {
-  __shared__ ZigShared zs;
+  __shared__ ZigShared32 zs;
   __shared__ unsigned long long item_s;
-  zig_stage(zs, g.tabs, false);
+  zig_stage32(zs, g.tabs);
   const SamplerCtx c{g.tabs, g.tabs->r32, g.tabs->r};
   unsigned err = 0;
   for (unsigned long long round = 0;; ++round) {

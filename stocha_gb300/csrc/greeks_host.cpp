@@ -433,6 +433,9 @@ int stocha_greeks_batch(stocha_ctx* ctx, const stocha_greeks_instance* inst, uin
       return set_error(STOCHA_ERR_VALUE, "instance " + std::to_string(i) + ": payoff must be call or put");
     if (x.n_paths == 0 || x.steps == 0)
       return set_error(STOCHA_ERR_VALUE, "instance " + std::to_string(i) + ": steps and n_paths must be positive");
+    // the FP32 batch kernel counts a path's normals in 32 bits
+    if (precision == STOCHA_FP32 && x.steps >= (1ull << 32))
+      return set_error(STOCHA_ERR_VALUE, "instance " + std::to_string(i) + ": steps must be below 2^32 in fp32");
   }
   int rc = resolve_ctx(&ctx);
   if (rc) return rc;

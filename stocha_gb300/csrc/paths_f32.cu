@@ -699,30 +699,6 @@ __device__ __forceinline__ WarpRow warp_row(const PathLaunch& a, uint64_t base) 
   return r;
 }
 
-// Iteration bound of one warp's rows: far above the ~1.03 draws per normal
-// (a warp that reaches it flags kErrZigAttempts and stops).  Counts are
-// 32-bit: the launcher sends only steps * assets < 2^24 here.
-__device__ __forceinline__ uint32_t uf_cap(uint32_t normals) { return 64 * normals + 4096; }
-
-// Calls feed() (one draw per lane) in groups of kUfUnroll until every lane's
-// count has reached its need; the warp vote runs once per group (8 draws a
-// group: measured on GB300 with ZigFeed, 3-asset sums 1.79 -> 1.71 ms over 4).
-constexpr int kUfUnroll = 8;
-template <int kU = kUfUnroll, class F>
-__device__ __forceinline__ void uf_drive(const uint32_t& cnt, uint32_t need, uint32_t cap, unsigned& err, F&& feed) {
-  uint32_t it = 0;
-#pragma unroll 1
-  while (__any_sync(0xFFFFFFFFu, cnt < need)) {
-    if (it >= cap) {
-      err |= kErrZigAttempts;
-      break;
-    }
-#pragma unroll
-    for (int j = 0; j < kU; ++j) feed();
-    it += kU;
-  }
-}
-
 // GBM (NA = 0) and multi-GBM with NA assets: only the per-asset sums of the
 // normals matter.  The sum being filled is always w[0]; after each normal the
 // sums rotate, so after steps * NA normals they are back in asset order.

@@ -227,6 +227,8 @@ int validate(const stocha_request& r) {
   if (x.payoff != STOCHA_PAYOFF_CALL && x.payoff != STOCHA_PAYOFF_PUT)
     return set_error(STOCHA_ERR_VALUE, "payoff must be call or put");
   if (x.n_paths == 0 || x.steps == 0) return set_error(STOCHA_ERR_VALUE, "steps and n_paths must be positive");
+  // the FP32 kernels count a path's normals in 32 bits
+  if (x.steps >= (1ull << 32)) return set_error(STOCHA_ERR_VALUE, "steps must be below 2^32");
   return STOCHA_OK;
 }
 

@@ -299,6 +299,14 @@ def test_tune_table_host_logic(stocha):
         stocha.tune_set("multi_gbm", 256, 1, 1, variant=0, n_assets=3)
 
 
+def test_greeks_batch_step_limit(stocha):
+    """The FP32 batch kernel counts a path's normals in 32 bits: an FP32
+    instance with 2^32 steps or more is a value error before any CUDA call."""
+    inst = dict(model="gbm", s0=100.0, sigma=0.2, r=0.05, t=1.0, strike=100.0, n_paths=1000, steps=2**32)
+    with pytest.raises(ValueError, match=r"instance 0: steps must be below 2\^32 in fp32"):
+        stocha.greeks_batch([inst], precision="fp32")
+
+
 def test_hull_white_validation(stocha):
     """hull_white's argument checks (lib.rs:617-636) happen before any CUDA call."""
     for kw, msg in [(dict(a=0.0), "a must be positive"), (dict(sigma=0.0), "sigma must be positive"),
