@@ -361,6 +361,7 @@ int stocha_var_cvar_device(stocha_ctx* ctx, const double* returns_dev, uint64_t 
  * 24 shapes.  stocha_autotune times every shape on the given model
  * and size (reps launches each, CUDA events on the context's stream) and
  * installs the fastest for that model kind; the table is process-wide.
+ * Before any tuning every kind uses variant 2, 256 threads, 2 waves.
  * Draws and per-path values do not depend on the shape; the grouping of the
  * FP32 payoff partial sums does (their last bits). */
 typedef struct stocha_tune_result {
@@ -368,7 +369,7 @@ typedef struct stocha_tune_result {
   int32_t block, ilp, waves, variant;
   int32_t candidates;      /* shapes timed */
   int32_t pad;
-  double ms_best, ms_default; /* per launch: the chosen shape, and variant 0 / 256 / 1 wave */
+  double ms_best, ms_default; /* per launch: the chosen shape, and the default (variant 2 / 256 / 2 waves) */
 } stocha_tune_result;
 
 int stocha_autotune(stocha_ctx* ctx, const stocha_model* m, int32_t reps, stocha_tune_result* out);

@@ -782,7 +782,7 @@ int stocha_autotune(stocha_ctx* ctx, const stocha_model* m, int32_t reps, stocha
         const FusedTune t{b, fm[1], waves, fm[0]};
         if ((rc = time_cfg(t, &ms))) break;
         ++n;
-        if (b == 256 && fm[0] == 0 && waves == 1) default_ms = ms;
+        if (b == 256 && fm[0] == 2 && fm[1] == 1 && waves == 2) default_ms = ms;  // the built-in default
         if (ms < best_ms) {
           best_ms = ms;
           best = t;

@@ -851,9 +851,13 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_merton_uf(const __grid_co
 }
 
 // Tuning table: per model kind (gbm, heston, merton, multi-GBM with 1..4
-// assets) the block size, ILP and grid waves of the fused launch.
-FusedTune g_tune[kTuneSlots] = {{256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0},
-                                {256, 1, 1, 0}, {256, 1, 1, 0}, {256, 1, 1, 0}};
+// assets) the block size, ILP, grid waves and kernel form of the fused
+// launch.  Default: the warp-uniform form (ZigFeed), 256 threads, 2 waves,
+// which the autotuner picks for all three models of the 1e6 x 252 workload on
+// GB300 (the shapes it prefers for the other block sizes and waves lie within
+// about 1 % of it).
+FusedTune g_tune[kTuneSlots] = {{256, 1, 2, 2}, {256, 1, 2, 2}, {256, 1, 2, 2}, {256, 1, 2, 2},
+                                {256, 1, 2, 2}, {256, 1, 2, 2}, {256, 1, 2, 2}};
 
 const void* fused_kernel(int slot, int ilp, int variant) {
   if (variant == 0) {  // the per-path loop kernels (one path per thread at a time)
@@ -958,7 +962,7 @@ int tune_slot(int model, int na) {
 }
 
 FusedTune get_fused_tune(int slot) {
-  return slot >= 0 && slot < kTuneSlots ? g_tune[slot] : FusedTune{256, 1, 1, 0};
+  return slot >= 0 && slot < kTuneSlots ? g_tune[slot] : FusedTune{256, 1, 2, 2};
 }
 
 int set_fused_tune(int slot, FusedTune t) {

@@ -280,6 +280,7 @@ def test_tune_table_host_logic(stocha):
     """The fused-kernel launch-shape table: valid shapes are installed and read
     back, invalid ones are refused with ValueError (no GPU involved)."""
     before = stocha.tune_get("gbm")
+    before_m3 = stocha.tune_get("multi_gbm", 3)
     try:
         stocha.tune_set("gbm", 128, 2, 2, variant=1)
         got = stocha.tune_get("gbm")
@@ -296,7 +297,8 @@ def test_tune_table_host_logic(stocha):
         assert stocha.tune_get("multi_gbm", 3)["block"] == 64
     finally:
         stocha.tune_set("gbm", before["block"], before["ilp"], before["waves"], variant=before["variant"])
-        stocha.tune_set("multi_gbm", 256, 1, 1, variant=0, n_assets=3)
+        stocha.tune_set("multi_gbm", before_m3["block"], before_m3["ilp"], before_m3["waves"],
+                        variant=before_m3["variant"], n_assets=3)
 
 
 def test_greeks_batch_step_limit(stocha):
