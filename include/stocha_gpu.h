@@ -133,6 +133,16 @@ int stocha_debug_fast_log_error(stocha_ctx* ctx, double* abs_err_half_to_one, do
  * cap named in stocha_last_error(); the next call starts clean. */
 int stocha_debug_capped_draws(stocha_ctx* ctx, int32_t sampler, int32_t cap, uint64_t seed, uint64_t n,
                               double* out);
+/* Diagnostic (no counterpart in the reference): the two FP32 samplers of the
+ * engine on the same streams.  Stream i < n_paths is the seed's stream
+ * advanced by i * (n + 1024) * 2 draws (gbm.rs:55-59); out[i * n + k] is its
+ * k-th normal and state[2 i], state[2 i + 1] the generator state (low, high
+ * words) after the last draw those n normals consumed (host buffers).
+ * form 0: the per-path loop sampler (normal_f32); form 1: the warp-uniform
+ * feed of the fused kernels (ZigFeed).  Both consume exactly the reference's
+ * draws (src/dist/normal.rs:18-67), so they must agree bit for bit. */
+int stocha_debug_zigfeed(stocha_ctx* ctx, int32_t form, uint64_t seed, uint64_t n_paths, uint32_t n, float* out,
+                         uint64_t* state);
 /* Diagnostic (no counterpart in the reference): measured peak rate of one
  * pipe for roofline denominators.  kind 0: FP32 FFMA flop/s, 1: FP64 DFMA
  * flop/s, 2: 32-bit IMAD op/s, 3: PCG64DXSM draws/s (generator alone). */

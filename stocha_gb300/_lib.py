@@ -154,6 +154,7 @@ SIGNATURES = [
     ("stocha_debug_sqrt", c_i32, [c_void_p, P_dbl, P_dbl, c_u64]),
     ("stocha_debug_f64", c_i32, [c_void_p, c_i32, P_dbl, P_dbl, c_u64]),
     ("stocha_debug_capped_draws", c_i32, [c_void_p, c_i32, c_i32, c_u64, c_u64, P_dbl]),
+    ("stocha_debug_zigfeed", c_i32, [c_void_p, c_i32, c_u64, c_u64, ctypes.c_uint32, c_void_p, c_void_p]),
     ("stocha_debug_fast_log_error", c_i32, [c_void_p, P_dbl, P_dbl]),
     ("stocha_measure_peak", c_i32, [c_void_p, c_i32, P_dbl]),
 ]

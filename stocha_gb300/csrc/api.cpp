@@ -880,6 +880,35 @@ int stocha_debug_capped_draws(stocha_ctx* ctx, int32_t sampler, int32_t cap, uin
   return finish_call(ctx);
 }
 
+int stocha_debug_zigfeed(stocha_ctx* ctx, int32_t form, uint64_t seed, uint64_t n_paths, uint32_t n, float* out,
+                         uint64_t* state) {
+  if (form < 0 || form > 1) return set_error(STOCHA_ERR_VALUE, "form must be 0 or 1");
+  if (!out || !state) return set_error(STOCHA_ERR_VALUE, "out and state must not be NULL");
+  int rc = resolve_ctx(&ctx);
+  if (rc) return rc;
+  if (n_paths == 0 || n == 0) return STOCHA_OK;
+  std::lock_guard<std::recursive_mutex> lk(ctx->mu);
+  DeviceGuard g(ctx->device);
+  const size_t vbytes = (size_t)n_paths * n * sizeof(float), sbytes = (size_t)n_paths * 2 * sizeof(uint64_t);
+  if ((rc = ensure_buf(ctx, ctx->aux, vbytes + sbytes))) return rc;
+  DebugZig a;
+  std::memset(&a, 0, sizeof a);
+  make_stream_spec((u128)seed, ((u128)n + 1024) * 2, &a.ss);  // GBM-style streams (gbm.rs:55)
+  a.tabs = ctx->d_tabs;
+  a.err = ctx->d_err;
+  a.out = (float*)ctx->aux.ptr;
+  a.state = (uint64_t*)((char*)ctx->aux.ptr + vbytes);
+  a.n_paths = n_paths;
+  a.n = n;
+  a.form = form;
+  if ((rc = begin_call(ctx))) return rc;
+  launch_debug_zigfeed(a, ctx->stream);
+  STOCHA_CUDA(cudaGetLastError());
+  STOCHA_CUDA(cudaMemcpyAsync(out, a.out, vbytes, cudaMemcpyDeviceToHost, ctx->stream));
+  STOCHA_CUDA(cudaMemcpyAsync(state, a.state, sbytes, cudaMemcpyDeviceToHost, ctx->stream));
+  return finish_call(ctx);
+}
+
 int stocha_debug_zig_thresholds(uint64_t* thr256) {
   ZigTables t;
   build_tables(&t);

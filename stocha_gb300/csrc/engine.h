@@ -132,6 +132,20 @@ void launch_debug_f64(int fn, const double* x, double* y, uint64_t n, const ZigT
 // out[0..1] (zeroed by the caller): float bits of the largest absolute error
 // of __logf on [0.5, 1) and of its largest relative error below 0.5.
 void launch_debug_logf_scan(unsigned* out, cudaStream_t st);
+
+// Diagnostic: n normals for each of n_paths streams from one of the FP32
+// samplers, and each stream's generator state after its last consumed draw.
+struct DebugZig {
+  StreamSpec ss;
+  const ZigTables* tabs;
+  unsigned* err;
+  float* out;         // [n_paths][n]
+  uint64_t* state;    // [n_paths][2]: lo, hi
+  uint64_t n_paths;
+  uint32_t n;
+  int form;           // 0: normal_f32 one normal after another; 1: ZigFeed, warp-uniform
+};
+void launch_debug_zigfeed(const DebugZig& a, cudaStream_t st);
 // Sum per-block partials (deterministic order) into out[nvals].
 void launch_reduce_partials(const double* partials, int nblocks, int nvals, double* out, cudaStream_t st);
 

@@ -1031,6 +1031,54 @@ int launch_paths_f32(const PathLaunch& L, cudaStream_t st) {
   return cudaPeekAtLastError() == cudaSuccess ? (int)g : -1;
 }
 
+// Diagnostic: the two FP32 sampler forms on the same streams (stream i:
+// path i of the launch's StreamSpec).  Form 0 calls normal_f32 n times per
+// thread; form 1 runs ZigFeed warp-uniformly (32 consecutive streams a warp)
+// and records a stream's generator state when its n-th normal completes.  Both
+// must give the same values and states bit for bit.
+__global__ void __launch_bounds__(256) k_debug_zigfeed(const __grid_constant__ DebugZig a) {
+  __shared__ ZigShared zs;
+  __shared__ ZigShared32 zs32;
+  zig_stage(zs, a.tabs, false);
+  zig_stage32(zs32, a.tabs);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t wb = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wb < a.n_paths; wb += nthreads) {
+    const uint64_t i = wb + (threadIdx.x & 31u);
+    const bool ok = i < a.n_paths;
+    DevPcg st = pcg_path_state(a.ss, ok ? i : wb);
+    float* out = a.out + (ok ? i : 0) * a.n;
+    if (a.form == 0) {
+      if (ok) {
+        PcgGen g{st, a.ss.inc_lo, a.ss.inc_hi};
+        for (uint32_t k = 0; k < a.n; ++k) out[k] = normal_f32(g, c, zs, err);
+        a.state[2 * i] = g.s.lo;
+        a.state[2 * i + 1] = g.s.hi;
+      }
+    } else {
+      ZigFeed q;
+      const uint32_t need = ok ? a.n : 0u;
+      uint32_t cnt = 0;
+      uf_drive(cnt, need, uf_cap(a.n), err, [&]() {
+        float z;
+        if (q.feed(pcg_next(st, a.ss.inc_lo, a.ss.inc_hi), zs32, c, z) & (cnt < need)) {
+          out[cnt] = z;
+          if (++cnt == need) {
+            a.state[2 * i] = st.lo;
+            a.state[2 * i + 1] = st.hi;
+          }
+        }
+      });
+    }
+  }
+  if (err) atomicOr(a.err, err);
+}
+
+void launch_debug_zigfeed(const DebugZig& a, cudaStream_t st) {
+  if (a.n_paths) k_debug_zigfeed<<<(unsigned)std::min<uint64_t>((a.n_paths + 255) / 256, 4096), 256, 0, st>>>(a);
+}
+
 void launch_debug_logf_scan(unsigned* out, cudaStream_t st) {
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
