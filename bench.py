@@ -553,6 +553,18 @@ DRAM_BYTES_PER_ROW = {"multi_gbm": (179.968e3 + 1160.567e6) / 2e5, "heston": (10
 #   Merton: normal product, exponent DFMA, price product (+3 on the ~0.4 % jump steps)
 FP64_OPS_PER_PATH_STEP = {"multi_gbm": 12.0, "heston": 9.0, "merton": 3.0 + 3.0 / 252}
 
+# Hardware-pipe figures of the FP32 fused kernels (warp-uniform form, default
+# launch shape), from one ncu --set full capture of 2e5-path launches: issue
+# slots busy, ALU and FMA pipe instruction rates (of their peaks), warp
+# instructions per PCG64DXSM draw and threads active per warp instruction.
+# They change only with the kernels; the capture's summary in this repository
+# is profiles/k_uf_fp32_fused_200k.md.
+FP32_FUSED_NCU = {
+    "multi_gbm": {"issue_active": 0.728, "alu": 0.523, "fma": 0.310, "warp_inst_per_draw": 62.1, "simt": 28.2},
+    "heston": {"issue_active": 0.721, "alu": 0.582, "fma": 0.303, "warp_inst_per_draw": 75.7, "simt": 28.0},
+    "merton": {"issue_active": 0.689, "alu": 0.503, "fma": 0.319, "warp_inst_per_draw": 56.4, "simt": 28.7},
+}
+
 
 def oracle_headline_step(cores):
     """One step of the headline workload on the host cores by the oracle (the
@@ -805,7 +817,7 @@ def run_ours(args, rank, world):
     fp32f = {"value": world * path_steps / (ms32 * 1e-3), "unit": "path-steps/s", "ms_per_step": ms32,
              "speedup_vs_fp64_plain": (world * path_steps / (ms32 * 1e-3)) / value,
              "kernel_ms": kms32, "autotune": tuning,
-             "roofline": {"bound": "integer pipes and issue (PCG64DXSM generator)",
+             "roofline": {"bound": "issue, ALU and FMA-heavy pipes (PCG64DXSM generator and sampler)",
                           "achieved": achieved_draws / 1e9, "unit": "G draws/s",
                           "generator_alone_peak": peak_draws.value / 1e9,
                           "frac_of_generator_alone": achieved_draws / peak_draws.value,
@@ -813,7 +825,9 @@ def run_ours(args, rank, world):
                           "measured_pipe_peaks": {"ffma_gflops": peaks["ffma_flops"] / 1e9,
                                                   "imad_gops": peaks["imad_ops"] / 1e9,
                                                   "dfma_gflops": peak_dfma.value / 1e9},
-                          "traffic": 77824, "traffic_unit": "bytes per launch (multi-GBM kernel: tables only)"},
+                          "traffic": 77824, "traffic_unit": "bytes per launch (multi-GBM kernel: tables only)",
+                          "ncu_pipes": dict(FP32_FUSED_NCU, source="ncu --set full on 2e5-path launches of the "
+                                            "warp-uniform kernels (profiles/k_uf_fp32_fused_200k.md)")},
              "config": "same three models, 1e6 paths x 252 steps, European call K=100 reduced in-kernel, FP32 "
                        "paths (<= 1e-4 relative price error vs FP64)"}
     if not args.skip_e2e:
