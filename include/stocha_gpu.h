@@ -33,6 +33,7 @@ extern "C" {
 #define STOCHA_ERR_CALLBACK 5 /* a user payoff callback reported failure */
 #define STOCHA_ERR_BUSY 6     /* serving: admission refused (memory budget) */
 #define STOCHA_ERR_TIMEOUT 7  /* serving: a wait ended before the request finished */
+#define STOCHA_ERR_CANCELLED 8 /* serving: the request was cancelled before it was admitted */
 
 #define STOCHA_FP64 0 /* the reference's algorithm in FP64: paths within 1e-12 of its output */
 #define STOCHA_FP32 1 /* FP32 paths, FP64 reductions */
@@ -429,6 +430,7 @@ typedef struct stocha_server_counters {
   uint64_t submitted, completed, failed, jobs, batched_requests;
   uint64_t budget_bytes, peak_bytes, in_use_bytes;
   int32_t lanes, high_lanes; /* high_lanes: lanes above the lowest priority */
+  uint64_t cancelled;
 } stocha_server_counters;
 
 int stocha_server_create(int32_t device, uint64_t budget_bytes, int32_t lanes, stocha_server** out);
@@ -437,6 +439,12 @@ int stocha_server_destroy(stocha_server* s);
 /* Validates (the reference's messages) and queues a request. */
 int stocha_server_submit(stocha_server* s, const stocha_request* req, uint64_t* ticket);
 int stocha_server_poll(stocha_server* s, uint64_t ticket, stocha_result* out);
+/* Cancels a request that has not been admitted yet (it still waits for a lane
+ * or for device memory): *cancelled = 1, and its result's status becomes
+ * -STOCHA_ERR_CANCELLED.  A request already admitted runs to completion:
+ * *cancelled = 0.  Admission and cancellation are ordered under the server's
+ * lock, so exactly one of them wins. */
+int stocha_server_cancel(stocha_server* s, uint64_t ticket, int32_t* cancelled);
 /* timeout_s < 0: wait without limit. */
 int stocha_server_wait(stocha_server* s, uint64_t ticket, double timeout_s, stocha_result* out);
 /* Open-loop load: submits reqs[i] at arrival_s[i] seconds after the call

@@ -21,6 +21,7 @@ STOCHA_ERR_DEVICE = 4
 STOCHA_ERR_CALLBACK = 5
 STOCHA_ERR_BUSY = 6
 STOCHA_ERR_TIMEOUT = 7
+STOCHA_ERR_CANCELLED = 8
 REQ_PRICE, REQ_GREEKS, REQ_LSMC = 0, 1, 2
 
 FP64, FP32 = 0, 1
@@ -73,7 +74,7 @@ class StochaResult(ctypes.Structure):
 class StochaServerCounters(ctypes.Structure):
     _fields_ = [(k, c_u64) for k in ("submitted", "completed", "failed", "jobs", "batched_requests",
                                      "budget_bytes", "peak_bytes", "in_use_bytes")] + \
-        [("lanes", c_i32), ("high_lanes", c_i32)]
+        [("lanes", c_i32), ("high_lanes", c_i32), ("cancelled", c_u64)]
 
 
 class StochaTuneResult(ctypes.Structure):
@@ -144,6 +145,7 @@ SIGNATURES = [
     ("stocha_server_destroy", c_i32, [c_void_p]),
     ("stocha_server_submit", c_i32, [c_void_p, ctypes.POINTER(StochaRequest), ctypes.POINTER(c_u64)]),
     ("stocha_server_poll", c_i32, [c_void_p, c_u64, ctypes.POINTER(StochaResult)]),
+    ("stocha_server_cancel", c_i32, [c_void_p, c_u64, ctypes.POINTER(c_i32)]),
     ("stocha_server_wait", c_i32, [c_void_p, c_u64, c_dbl, ctypes.POINTER(StochaResult)]),
     ("stocha_server_replay", c_i32, [c_void_p, ctypes.POINTER(StochaRequest), P_dbl, c_u64,
                                      ctypes.POINTER(StochaResult)]),

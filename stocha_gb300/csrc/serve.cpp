@@ -118,12 +118,17 @@ double now_s(std::chrono::steady_clock::time_point t0) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// Where a request is: queued (submitted, not admitted), admitted (its job is
+// on a lane or done) or cancelled before admission.
+enum : uint8_t { kQueued = 0, kAdmitted = 1, kCancelled = 2 };
+
 struct Req {
   stocha_request r;
   stocha_result res;
   uint64_t bytes = 0;  // arena bytes of its job when run alone
   bool small = false;
   bool lsmc = false;
+  uint8_t phase = kQueued;  // under the server's lock
 };
 
 // A request as the dispatcher sees it (its own copy, taken under the lock).
@@ -175,6 +180,7 @@ struct stocha_server {
   // dispatcher-only state
   std::deque<Pending> pending;  // seen, not admitted (submission order)
   uint64_t jobs = 0, batched = 0, completed = 0, failed = 0;
+  uint64_t cancelled = 0;  // under the lock
 
   void loop();
   bool poll_lanes();
@@ -182,6 +188,7 @@ struct stocha_server {
   bool launch_batch(Lane& L, const std::vector<const Pending*>& t, uint64_t off, uint64_t items);
   bool launch_lsmc(Lane& L, const Pending& p, uint64_t off);
   void fail(const std::vector<uint64_t>& t, int code, const std::string& msg);
+  std::vector<const Pending*> claim(const std::vector<const Pending*>& t);
 };
 
 namespace {
@@ -395,9 +402,37 @@ bool stocha_server::poll_lanes() {
 
 // Admits pending requests onto free lanes while their bytes fit; true if
 // anything was launched.
+// Admits the requests of t that were not cancelled: under the lock, so that a
+// cancel either comes first (the request is dropped here) or finds it
+// admitted.  Stamps their admission time.
+std::vector<const Pending*> stocha_server::claim(const std::vector<const Pending*>& t) {
+  std::vector<const Pending*> out;
+  std::lock_guard<std::mutex> lk(mu);
+  const double now = now_s(t0);
+  for (const Pending* p : t) {
+    Req& r = reqs[p->ticket];
+    if (r.phase == kCancelled) continue;
+    r.phase = kAdmitted;
+    r.res.t_admit = now;
+    out.push_back(p);
+  }
+  return out;
+}
+
 bool stocha_server::dispatch() {
   if (pending.empty()) return false;
   bool progress = false;
+  {  // requests cancelled while queued leave the queue
+    std::lock_guard<std::mutex> lk(mu);
+    std::deque<Pending> keep;
+    for (Pending& p : pending)
+      if (reqs[p.ticket].phase != kCancelled) keep.push_back(p);
+    if (keep.size() != pending.size()) {
+      pending.swap(keep);
+      progress = true;
+    }
+  }
+  if (pending.empty()) return progress;
   auto free_lane = [&](int cls) -> Lane* {
     for (Lane& L : lanes)
       if (!L.busy && L.cls == cls) return &L;
@@ -410,11 +445,6 @@ bool stocha_server::dispatch() {
     if (!small) return free_lane(lsmc ? kMid : kLow);
     Lane* L = free_lane(lsmc ? kMid : kHigh);
     return L ? L : free_lane(lsmc ? kHigh : kMid);
-  };
-  auto stamp_admit = [&](const std::vector<const Pending*>& t) {
-    std::lock_guard<std::mutex> lk(mu);
-    const double now = now_s(t0);
-    for (const Pending* p : t) reqs[p->ticket].res.t_admit = now;
   };
   std::vector<bool> taken(pending.size(), false);
   // 1. one batch of the small pricing/Greeks requests (highest priority; a
@@ -437,10 +467,12 @@ bool stocha_server::dispatch() {
     Lane* L = t.empty() ? nullptr : lane_for(true, false);
     uint64_t off = 0;
     if (L && arena.alloc(batch_bytes(t.size(), items), &off)) {
-      stamp_admit(t);
-      if (!launch_batch(*L, t, off, items)) arena.release(off);
+      const std::vector<const Pending*> c = claim(t);
+      uint64_t citems = 0;
+      for (const Pending* p : c) citems += items_of(p->q);
+      if (c.empty() || !launch_batch(*L, c, off, citems)) arena.release(off);
       for (size_t i : idx) taken[i] = true;
-      batched += t.size();
+      batched += c.size();
       progress = true;
     }
   }
@@ -456,8 +488,8 @@ bool stocha_server::dispatch() {
     if (!L) continue;
     uint64_t off = 0;
     if (!arena.alloc(q.bytes, &off)) continue;
-    stamp_admit({&p});
-    const bool ok = q.lsmc ? launch_lsmc(*L, p, off) : launch_batch(*L, {&p}, off, items_of(q));
+    const bool admitted = !claim({&p}).empty();
+    const bool ok = admitted && (q.lsmc ? launch_lsmc(*L, p, off) : launch_batch(*L, {&p}, off, items_of(q)));
     if (!ok) arena.release(off);
     taken[i] = true;
     progress = true;
@@ -608,6 +640,28 @@ int stocha_server_poll(stocha_server* s, uint64_t ticket, stocha_result* out) {
   return STOCHA_OK;
 }
 
+int stocha_server_cancel(stocha_server* s, uint64_t ticket, int32_t* cancelled) {
+  if (!s || !cancelled) return set_error(STOCHA_ERR_VALUE, "server and cancelled must not be NULL");
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (ticket >= s->reqs.size()) return set_error(STOCHA_ERR_VALUE, "unknown ticket");
+    Req& r = s->reqs[ticket];
+    if (r.phase == kAdmitted) {
+      *cancelled = 0;  // on a lane or done: it runs to completion
+      return STOCHA_OK;
+    }
+    *cancelled = 1;
+    if (r.phase == kCancelled) return STOCHA_OK;
+    r.phase = kCancelled;
+    r.res.status = -STOCHA_ERR_CANCELLED;
+    r.res.t_done = now_s(s->t0);
+    ++s->cancelled;
+  }
+  s->cv_done.notify_all();
+  s->cv_in.notify_one();  // the dispatcher drops it from its queue
+  return STOCHA_OK;
+}
+
 int stocha_server_wait(stocha_server* s, uint64_t ticket, double timeout_s, stocha_result* out) {
   if (!s || !out) return set_error(STOCHA_ERR_VALUE, "server and out must not be NULL");
   std::unique_lock<std::mutex> lk(s->mu);
@@ -661,6 +715,7 @@ int stocha_server_stats(stocha_server* s, stocha_server_counters* out) {
   out->submitted = s->reqs.size();
   out->completed = s->completed;
   out->failed = s->failed;
+  out->cancelled = s->cancelled;
   out->jobs = s->jobs;
   out->batched_requests = s->batched;
   out->budget_bytes = s->arena.capacity();

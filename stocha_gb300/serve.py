@@ -65,7 +65,8 @@ def _fill(x: _lib.StochaRequest, d: dict) -> None:
 
 
 def _result(r: _lib.StochaResult, kind: int) -> dict:
-    out = {"status": "done" if r.status == 1 else ("pending" if r.status == 0 else "failed"),
+    status = {1: "done", 0: "pending", -_lib.STOCHA_ERR_CANCELLED: "cancelled"}.get(r.status, "failed")
+    out = {"status": status,
            "price": r.price, "std_err": r.std_err,
            "t_submit": r.t_submit, "t_admit": r.t_admit, "t_done": r.t_done}
     if r.status < 0:
@@ -123,6 +124,14 @@ class Server:
         r = _lib.StochaResult()
         _lib.check(self._lib.stocha_server_poll(self._h, int(ticket), ctypes.byref(r)))
         return _result(r, self._kinds.get(ticket, -1))
+
+    def cancel(self, ticket: int) -> bool:
+        """Cancels a request that is still waiting for admission (a lane or
+        device memory); True if it is (now) cancelled, False if it was already
+        admitted, in which case it runs to completion."""
+        c = ctypes.c_int32()
+        _lib.check(self._lib.stocha_server_cancel(self._h, int(ticket), ctypes.byref(c)))
+        return bool(c.value)
 
     def wait(self, ticket: int, timeout: float | None = None) -> dict:
         r = _lib.StochaResult()

@@ -9,6 +9,9 @@
 * Admission by device memory: a budget that holds one LSMC job at a time
   still completes every request, never holds more than the budget, and a
   request larger than the budget is refused at submission.
+* Failures made on the host: a request cancelled while it waits for
+  admission never runs; a budget the device cannot allocate fails creation
+  with MemoryError and leaves the process able to serve.
 """
 import numpy as np
 import pytest
@@ -112,6 +115,48 @@ def test_admission_by_memory_budget(stocha):
     for (a0, d0), (a1, d1) in zip(spans, spans[1:]):
         assert a1 >= d0 - 1e-3 or a1 >= a0  # admitted after the previous finished (poll granularity)
     assert len({r["price"] for r in res}) == 6  # different seeds, different prices
+
+
+def test_cancel_waiting_request(stocha):
+    """A request still waiting for admission can be cancelled: its result is
+    'cancelled', it never runs, and the server goes on serving.  A request
+    already admitted is not: cancel returns False and it completes.  With a
+    budget that holds one LSMC job (each holds ~4e6 * 253 * 4 bytes of paths)
+    the second one waits while the first runs (~15 ms on GB300); the cancel
+    comes microseconds after its submission."""
+    big = dict(kind="lsmc", payoff="put", s0=100.0, r=0.05, sigma=0.2, t=1.0, strike=100.0, n_paths=4_000_000,
+               steps=252, poly_degree=3)
+    budget = 6 << 30
+    with stocha.Server(budget_bytes=budget, lanes=8) as srv:
+        t0 = srv.submit(big)
+        t1 = srv.submit(dict(big, seed=7))
+        assert srv.cancel(t1) is True
+        assert srv.cancel(t1) is True  # idempotent
+        r1 = srv.wait(t1)
+        r0 = srv.wait(t0)
+        assert srv.cancel(t0) is False  # admitted and done
+        small = srv.submit(dict(kind="price", model="gbm", s0=100.0, r=0.05, sigma=0.2, t=1.0, strike=100.0,
+                                n_paths=10_000, steps=12))
+        r2 = srv.wait(small)
+        st = srv.stats()
+    assert r1["status"] == "cancelled" and r1["t_admit"] == 0.0
+    assert r0["status"] == "done" and r2["status"] == "done"
+    assert st["cancelled"] == 1 and st["failed"] == 0 and st["completed"] == 2
+    with pytest.raises(ValueError, match="unknown ticket"):
+        with stocha.Server(budget_bytes=64 << 20, lanes=3) as srv:
+            srv.cancel(5)
+
+
+def test_budget_allocation_failure(stocha):
+    """A serving budget beyond the device's memory: the slab's cudaMalloc
+    fails, creation raises MemoryError naming the budget, and the process's
+    CUDA context stays usable for a server that fits."""
+    with pytest.raises(MemoryError, match="device allocation of the serving budget"):
+        stocha.Server(budget_bytes=1 << 50, lanes=3)
+    with stocha.Server(budget_bytes=64 << 20, lanes=3) as srv:
+        r = srv.wait(srv.submit(dict(kind="price", model="gbm", s0=100.0, r=0.05, sigma=0.2, t=1.0, strike=100.0,
+                                     n_paths=10_000, steps=12)))
+    assert r["status"] == "done"
 
 
 def test_submit_validation(stocha):
