@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_multi_f
 
 // ------------------------------------------------ fused, warp-uniform -------
 // The same fused pricing with the ziggurat fed one draw per iteration
-// (zig_feed): each iteration every lane of the warp takes one generator step
+// (ZigFeed): each iteration every lane of the warp takes one generator step
 // and feeds it to its own sampler state; a lane that completes a normal hands
 // it to the model.  A warp prices 32 consecutive rows together and iterates
 // until all 32 have their normals (a lane that is done keeps stepping a
