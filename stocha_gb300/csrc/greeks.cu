@@ -98,6 +98,12 @@ __device__ __forceinline__ void contribute(const GInst& I, float S, float S_sp, 
   acc[8].add(pay(sm, I.K, call));
 }
 
+// Draws per warp vote in the feed loops.  This kernel holds the three models,
+// each in a price-only and a Greeks form, and with the fused kernels' 8 draws
+// a vote its code outgrew the instruction cache (ncu: instruction fetch the
+// top stall); 4 took the 512-instance batch from 77.7 to 66.2 ms on GB300.
+constexpr int kGreeksUnroll = 4;
+
 // The paths of a warp are 32 consecutive ones (base + lane), simulated with
 // the warp-uniform sampler feed (ZigFeed): every lane steps its generator in
 // the same instruction each iteration and only wedge tests and the tail
@@ -116,7 +122,7 @@ __device__ void path_gbm(const GInst& I, uint64_t p, bool ok, const SamplerCtx& 
   float W = 0.0f;
   const uint32_t need = ok ? (uint32_t)I.steps : 0u;
   uint32_t cnt = 0;
-  uf_drive(cnt, need, uf_cap(I.steps), err, [&]() {
+  uf_drive<kGreeksUnroll>(cnt, need, uf_cap(I.steps), err, [&]() {
     float z;
     if (q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z) & (cnt < need)) {
       W += z;
@@ -143,7 +149,7 @@ __device__ void merton_pass(const GInst& I, uint64_t p, bool ok, uint64_t thr, c
   bool in_jump = false;
   const uint32_t need = ok ? (uint32_t)I.steps : 0u;
   uint32_t cnt = 0;
-  uf_drive(cnt, need, uf_cap(2 * I.steps), err, [&]() {
+  uf_drive<kGreeksUnroll>(cnt, need, uf_cap(2 * I.steps), err, [&]() {
     float z;
     if (q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z) & (cnt < need)) {
       if (in_jump) {
@@ -208,7 +214,7 @@ __device__ void path_heston(const GInst& I, uint64_t p, bool ok, const SamplerCt
   bool half = false;
   const uint32_t need = ok ? (uint32_t)I.steps : 0u;
   uint32_t cnt = 0;
-  uf_drive<kUfUnroll / 2>(cnt, need, uf_cap(2 * I.steps), err, [&]() {
+  uf_drive<kGreeksUnroll / 2>(cnt, need, uf_cap(2 * I.steps), err, [&]() {
     float z1, z2;
     const bool a1 = q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z1);
     const bool a2 = q.feed(pcg_next(st, I.ss.inc_lo, I.ss.inc_hi), zs, c, z2);
