@@ -99,9 +99,9 @@ __device__ __forceinline__ void contribute(const GInst& I, float S, float S_sp, 
 }
 
 // Draws per warp vote in the feed loops.  This kernel holds the three models,
-// each in a price-only and a Greeks form, and with the fused kernels' 8 draws
-// a vote its code outgrew the instruction cache (ncu: instruction fetch the
-// top stall); 4 took the 512-instance batch from 77.7 to 66.2 ms on GB300.
+// each in a price-only and a Greeks form; with 8 draws a vote its code outgrew
+// the instruction cache (ncu: instruction fetch the top stall).  Measured on
+// GB300, 512-instance batch: 8 draws 77.7 ms, 4 draws 66.1 ms, 2 draws 67.6 ms.
 constexpr int kGreeksUnroll = 4;
 
 // The paths of a warp are 32 consecutive ones (base + lane), simulated with
