@@ -540,8 +540,8 @@ FLOPS_PER_PATH_STEP = {"multi_gbm": 24.0, "heston": 21.0, "merton": 7.0, "gbm": 
 # row count.  Dirty data still in L2 when a
 # capture ends is not counted, so these sit slightly below the algorithmic
 # 8 * 253 * width bytes a row.
-DRAM_BYTES_PER_ROW = {"multi_gbm": (179.968e3 + 1160.567e6) / 2e5, "heston": (104.960e3 + 351.270e6) / 2e5,
-                      "merton": (0.15e6 + 348.2e6) / 2e5}
+DRAM_BYTES_PER_ROW = {"multi_gbm": (0.112640e6 + 1164.697e6) / 2e5, "heston": (0.118528e6 + 354.099e6) / 2e5,
+                      "merton": (1.749760e6 + 354.970e6) / 2e5}
 
 # FP64 pipe operations per path-step that each FP64 plain kernel issues
 # (DMUL, DADD, DFMA counted once), read from the kernels: the exponential,
