@@ -54,7 +54,9 @@ struct Plain {
 // dependent-issue latency, and the values the cap spills belong to the rare
 // wedge and tail paths (measured on GB300: multi-GBM 2.97 -> 2.74 ms, Heston
 // 2.08 -> 2.02 ms, Merton 1.52 -> 1.48 ms; 6 blocks spilled into the common
-// path).  The warp-uniform multi-asset form carries more state: 4 blocks.
+// path).  The warp-uniform forms carry more state (the sampler feed's pending
+// draw and value): 4 blocks, 64 registers (a 56-register cap measured within
+// noise, 48 spilled on the common path).
 constexpr int kFusedMinBlocks = 5;
 constexpr int kUfMinBlocks = 4;
 // The materialised and element-store forms (staged row store, time-major
@@ -680,10 +682,10 @@ __global__ void __launch_bounds__(256, ILP == 1 ? kFusedMinBlocks : 1) k_multi_f
 // above; only the interleaving of lanes changes.
 
 // Rows of one warp: base (warp-uniform) + lane.  A lane past the end runs on
-// the first row's stream and contributes nothing.
-// The kernels draw with pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi): the stream
-// increment is read from the launch parameters at every draw (it stays in the
-// constant bank instead of four registers of every lane).
+// the first row's stream and contributes nothing.  The kernels draw with
+// pcg_next(r.st, a.ss.inc_lo, a.ss.inc_hi), reading the stream increment from
+// the launch parameters at every draw (the constant bank, not four registers
+// of every lane).
 struct WarpRow {
   bool ok, neg;
   DevPcg st;
