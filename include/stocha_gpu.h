@@ -141,7 +141,8 @@ int stocha_debug_capped_draws(stocha_ctx* ctx, int32_t sampler, int32_t cap, uin
  * words) after the last draw those n normals consumed (host buffers).
  * form 0: the per-path loop sampler (normal_f32); form 1: the warp-uniform
  * feed of the fused kernels (ZigFeed).  Both consume exactly the reference's
- * draws (src/dist/normal.rs:18-67), so they must agree bit for bit. */
+ * draws (src/dist/normal.rs:18-67), so they must agree bit for bit.
+ * n_paths * n at most 2^36. */
 int stocha_debug_zigfeed(stocha_ctx* ctx, int32_t form, uint64_t seed, uint64_t n_paths, uint32_t n, float* out,
                          uint64_t* state);
 /* Diagnostic (no counterpart in the reference): measured peak rate of one

@@ -887,6 +887,7 @@ int stocha_debug_zigfeed(stocha_ctx* ctx, int32_t form, uint64_t seed, uint64_t 
   int rc = resolve_ctx(&ctx);
   if (rc) return rc;
   if (n_paths == 0 || n == 0) return STOCHA_OK;
+  if (n_paths > (1ull << 36) / n) return set_error(STOCHA_ERR_VALUE, "n_paths * n must be at most 2^36");
   std::lock_guard<std::recursive_mutex> lk(ctx->mu);
   DeviceGuard g(ctx->device);
   const size_t vbytes = (size_t)n_paths * n * sizeof(float), sbytes = (size_t)n_paths * 2 * sizeof(uint64_t);
