@@ -852,6 +852,120 @@ __global__ void __launch_bounds__(256, kUfMinBlocks) k_merton_uf(const __grid_co
   if (err) atomicOr(a.err, err);
 }
 
+// ------------------------------------- materialised rows, warp-uniform -----
+// Heston (Euler) and Merton paths written row by row through the staged
+// sector writer, on the warp-uniform sampler feed.  A step completes at most
+// once a call (Heston: two draws a call, the step's normals picked by the
+// lane's phase; Merton: the jump uniform in the diffusion normal's call), and
+// its arithmetic and compensated sums are those of k_heston_euler_f32 and
+// k_merton_f32, so the rows are the same floats.  Lanes drift out of phase
+// after rejected attempts, so each lane puts its values as its steps complete
+// (the writer keeps a ring per lane); the warp ends its 32 rows together.
+__global__ void __launch_bounds__(256, kMatMinBlocks) k_heston_rows_uf(const __grid_constant__ PathLaunch a) {
+  PathOut<float, kRows> out;
+  out.init(dyn_smem);
+  __shared__ ZigShared32 zs;
+  zig_stage32(zs, a.tabs);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const F32K& f = a.f32;
+  const float rho = f.h_rho, rho_comp = f.h_rho_comp, kappa_dt = f.h_kdt;
+  const float theta = f.h_theta, xi_sdt = f.h_xsdt, sdt = f.h_sdt;
+  const float mu_dt = f.h_mudt, nhalf_dt = f.h_nhdt, s0 = f.h_s0;
+  unsigned err = 0;
+  for_rows_warp(a.rows, out, [&](uint64_t lrow, bool on) {
+    DevPcg st = pcg_path_state(a.ss, a.row_begin + lrow);
+    ZigFeed q;
+    float v = f.h_v0, zc = 0.0f;
+    Kahan lg;
+    bool half = false;
+    if (on) {
+      out.begin(a.out_f32 + lrow * (a.steps + 1));
+      out.rs.put(s0);
+    }
+    const uint32_t need = on ? (uint32_t)a.steps : 0u;
+    uint32_t cnt = 0;
+    uf_drive<kUfUnroll / 2>(cnt, need, uf_cap(2 * a.steps), err, [&]() {
+      float z1, z2;
+      const bool a1 = q.feed(pcg_next(st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z1);
+      const bool a2 = q.feed(pcg_next(st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z2);
+      const float first = a1 ? z1 : z2;
+      const bool two = a1 & a2, one = a1 ^ a2;
+      const bool step = half ? (a1 | a2) : two;
+      const float dw1 = half ? zc : z1;
+      const float dz = half ? first : z2;
+      if (half) {
+        if (two) zc = z2;
+      } else if (one) {
+        zc = first;
+      }
+      half ^= one;
+      if (step & (cnt < need)) {
+        const float dw2 = fmaf(rho, dw1, rho_comp * dz);
+        const float v_plus = fmaxf(v, 0.0f);
+        const float sqrt_v = sqrt_approx(v_plus);
+        v += fmaf(kappa_dt, theta - v_plus, xi_sdt * sqrt_v * dw2);
+        lg.add(fmaf(nhalf_dt, v_plus, mu_dt) + sqrt_v * sdt * dw1);
+        out.rs.put(s0 * expf(lg.value()));
+        ++cnt;
+      }
+    });
+  });
+  if (err) atomicOr(a.err, err);
+}
+
+__global__ void __launch_bounds__(256, kMatMinBlocks) k_merton_rows_uf(const __grid_constant__ PathLaunch a) {
+  PathOut<float, kRows> out;
+  out.init(dyn_smem);
+  __shared__ ZigShared32 zs;
+  zig_stage32(zs, a.tabs);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  const uint64_t thr = a.merton.jump_thr;
+  const float drift = a.f32.m_drift, diffusion = a.f32.m_diff, mu_j = a.f32.m_mu_j;
+  const float sigma_j = a.f32.m_sigma_j, s0 = a.f32.m_s0;
+  unsigned err = 0;
+  for_rows_warp(a.rows, out, [&](uint64_t lrow, bool on) {
+    DevPcg st = pcg_path_state(a.ss, a.row_begin + lrow);
+    ZigFeed q;
+    Kahan w;
+    float jumps = 0.0f, kf = 0.0f;
+    bool in_jump = false;
+    if (on) {
+      out.begin(a.out_f32 + lrow * (a.steps + 1));
+      out.rs.put(s0);
+    }
+    const uint32_t need = on ? (uint32_t)a.steps : 0u;
+    uint32_t cnt = 0;
+    uf_drive(cnt, need, uf_cap(2 * a.steps), err, [&]() {
+      float z;
+      if (q.feed(pcg_next(st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z) & (cnt < need)) {
+        bool done = true;
+        if (in_jump) {
+          jumps += fmaf(sigma_j, z, mu_j);
+          in_jump = false;
+        } else {
+          w.add(z);
+          if ((pcg_next(st, a.ss.inc_lo, a.ss.inc_hi) >> 11) < thr) {
+            in_jump = true;
+            done = false;
+          }
+        }
+        if (done) {
+          kf += 1.0f;
+          out.rs.put(s0 * expf(fmaf(kf, drift, diffusion * w.value()) + jumps));
+          ++cnt;
+        }
+      }
+    });
+  });
+  if (err) atomicOr(a.err, err);
+}
+
+// Materialised rows of Heston Euler and Merton go to the warp-uniform kernels
+// (their counts are 32-bit).
+inline bool rows_uf(const PathLaunch& L) {
+  return L.steps < (1ull << 31) && (L.model == kMerton || (L.model == kHeston && L.heston.scheme == 0));
+}
+
 // Tuning table: per model kind (gbm, heston, merton, multi-GBM with 1..4
 // assets) the block size, ILP, grid waves and kernel form of the fused
 // launch.  Default: the warp-uniform form (ZigFeed), 256 threads, 2 waves,
@@ -910,6 +1024,9 @@ void launch_multi32(const PathLaunch& L, dim3 g, dim3 b, size_t sm, cudaStream_t
 // The untuned kernel of L's model in store mode kMode (occupancy query).
 template <int kMode>
 const void* model_kernel32(const PathLaunch& L) {
+  if constexpr (kMode == kRows) {
+    if (rows_uf(L)) return L.model == kMerton ? (const void*)k_merton_rows_uf : (const void*)k_heston_rows_uf;
+  }
   switch (L.model) {
     case kGbm: return (const void*)k_gbm_f32<kMode>;
     case kHeston:
@@ -921,6 +1038,15 @@ const void* model_kernel32(const PathLaunch& L) {
 
 template <int kMode>
 int launch_model32(const PathLaunch& L, dim3 G, dim3 B, size_t sm, cudaStream_t st) {
+  if constexpr (kMode == kRows) {
+    if (rows_uf(L)) {
+      if (L.model == kMerton)
+        k_merton_rows_uf<<<G, B, sm, st>>>(L);
+      else
+        k_heston_rows_uf<<<G, B, sm, st>>>(L);
+      return 0;
+    }
+  }
   switch (L.model) {
     case kGbm: k_gbm_f32<kMode><<<G, B, sm, st>>>(L); break;
     case kHeston:

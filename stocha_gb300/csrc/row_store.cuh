@@ -162,4 +162,19 @@ __device__ __forceinline__ void for_rows(uint64_t rows, PathOut<T, kMode>& out, 
   }
 }
 
+// The same rows for the warp-uniform kernels: body(lrow, on) is called by all
+// 32 lanes of each warp (on: the lane has a row; lrow is then its row, else
+// the warp's first row), because the sampler feed inside votes across the
+// warp.  The loop runs warp-uniformly in every mode.
+template <typename T, int kMode, class Body>
+__device__ __forceinline__ void for_rows_warp(uint64_t rows, PathOut<T, kMode>& out, Body&& body) {
+  const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t wb = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wb < rows; wb += nthreads) {
+    const uint64_t lrow = wb + (threadIdx.x & 31u);
+    const bool on = lrow < rows;
+    body(on ? lrow : wb, on);
+    if constexpr (kMode == kRows) out.rs.end(on, lrow + 1 < rows);
+  }
+}
+
 }  // namespace stocha
