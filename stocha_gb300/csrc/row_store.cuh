@@ -21,9 +21,11 @@
 //   share the first sector with the previous row.  3 KB per warp.
 // Sector-relative offset o = ph + j of the row's element j, where ph is the
 // row's offset in its first sector; element j lives in ring slot o mod 2 SE.
-// Every SE puts (the same put for every lane of the warp, whatever the number
-// of values per step) the writer flushes the one sector completed since the
-// last flush, so the sector stores of all lanes issue together.
+// Every SE puts the writer flushes the one sector completed since the last
+// flush.  In the per-path loop kernels every lane of the warp makes the same
+// put at once (whatever the number of values per step), so the sector stores
+// of all lanes issue together; in the warp-uniform kernels each lane puts as
+// its own steps complete, and its ring and writes are its own.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -80,8 +82,8 @@ struct RowStore {
     }
   }
 
-  // Every SE puts (the same put for every lane of the warp) exactly one
-  // sector boundary has been crossed since the last write: write that sector.
+  // Every SE puts of this lane exactly one sector boundary has been crossed
+  // since its last write: write that sector.
   __device__ __forceinline__ void put(T v) {
     slot(o & (RING - 1)) = v;
     ++o;
