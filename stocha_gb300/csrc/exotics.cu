@@ -134,7 +134,9 @@ __global__ void __launch_bounds__(128) k_exotic(const __grid_constant__ ExoticLa
 // one exp per path; the Asian average takes one FP32 exp per step.  Values
 // differ from the FP64 form by rounding: a barrier decision can flip only for
 // a path within ~1e-7 (in log price) of the barrier at a monitoring date.
-__global__ void __launch_bounds__(128) k_exotic_f32(const __grid_constant__ ExoticLaunch a) {
+// The per-path loop form of k_exotic_f32, for step counts of 2^31 and more
+// (the warp-uniform form counts normals in 32 bits).
+__global__ void __launch_bounds__(128) k_exotic_f32_loop(const __grid_constant__ ExoticLaunch a) {
   __shared__ ZigShared zs;
   zig_stage(zs, a.tabs, false);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
@@ -238,6 +240,96 @@ __global__ void k_asian_means(const double* __restrict__ totals, uint64_t n, dou
   }
 }
 
+// FP32 exotic Monte Carlo on the warp-uniform sampler feed (ZigFeed): a warp
+// simulates 32 paths together, every lane stepping its generator each
+// iteration, and only wedge tests and tail draws diverge.  Each thread takes
+// the paths of the per-path loop form (path i on thread i mod the grid's
+// threads), and the normals, their order and every per-path update are the
+// loop form's, so the per-thread sums and the block totals are the same bits.
+// A knocked-out barrier path stops drawing (its lane needs no more normals);
+// a knock-in path draws to maturity.
+__global__ void __launch_bounds__(128) k_exotic_f32(const __grid_constant__ ExoticLaunch a) {
+  __shared__ ZigShared32 zs;
+  zig_stage32(zs, a.tabs);
+  const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
+  unsigned err = 0;
+  double sum = 0.0;
+  const float drift = a.f_drift, diffusion = a.f_diff, s0 = a.f_s0, k = a.f_k, lb = a.f_lb;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint32_t steps = (uint32_t)a.steps;
+  for (uint64_t wb = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); wb < a.n; wb += stride) {
+    const uint64_t i = wb + (threadIdx.x & 31u);
+    const bool on = i < a.n;
+    DevPcg st = pcg_path_state(a.ss, on ? i : wb);
+    ZigFeed q;
+    float ls = 0.0f;
+    int hit = -1;  // barrier: the monitoring step of the first crossing
+    float lmx = a.f_lm0, lmn = a.f_ln0;  // lookback
+    float sum_arith = 0.0f, sum_log = 0.0f;  // Asian
+    uint32_t need = on ? steps : 0u;
+    if (a.kind == kExoBarrier && a.already_hit) {
+      hit = 0;
+      if (!a.kind_in) need = 0;  // knocked out before the first step: nothing to draw
+    }
+    uint32_t cnt = 0;
+    uf_drive(cnt, need, uf_cap(a.steps), err, [&]() {
+      float z;
+      if (q.feed(pcg_next(st, a.ss.inc_lo, a.ss.inc_hi), zs, c, z) & (cnt < need)) {
+        ls += fmaf(diffusion, z, drift);
+        ++cnt;
+        if (a.kind == kExoBarrier) {
+          if (hit < 0 && (a.direction == 0 ? ls >= lb : ls <= lb)) {
+            hit = (int)cnt;
+            if (!a.kind_in) need = cnt;  // knocked out: stop drawing
+          }
+        } else if (a.kind == kExoLookback) {
+          lmx = fmaxf(lmx, ls);
+          lmn = fminf(lmn, ls);
+        } else {
+          sum_arith += expf(ls);
+          sum_log += ls;
+        }
+      }
+    });
+    if (!on) continue;
+    if (a.kind == kExoBarrier) {
+      const bool knocked = hit >= 0;
+      const float sT = s0 * expf(ls);
+      const float iv = a.is_call ? fmaxf(sT - k, 0.0f) : fmaxf(k - sT, 0.0f);
+      const float opt = a.kind_in ? (knocked ? iv : 0.0f) : (knocked ? 0.0f : iv);
+      sum += a.rebate == 0.0 ? (double)opt : (double)opt + rebate_pv(a, hit) / a.discount;
+    } else if (a.kind == kExoLookback) {
+      const float s = s0 * expf(ls), mx = s0 * expf(lmx), mn = s0 * expf(lmn);
+      sum += a.strike_fixed ? (a.is_call ? fmaxf(mx - k, 0.0f) : fmaxf(k - mn, 0.0f))
+                            : (a.is_call ? s - mn : mx - s);
+    } else {  // Asian: plain (per-path pair) or floating seasoned (block sum)
+      const double nsteps = (double)a.steps;
+      const double s = (double)s0 * exp((double)ls);
+      const double avg_a = a.s0 * (double)sum_arith / nsteps;
+      const double avg_g = a.s0 * exp((double)sum_log / nsteps);
+      if (a.kind == kExoAsian) {
+        double pa, pg;
+        if (!a.strike_floating) {
+          pa = intrinsic(avg_a, a.k, a.is_call);
+          pg = intrinsic(avg_g, a.k, a.is_call);
+        } else {
+          pa = a.is_call ? fmax(s - avg_a, 0.0) : fmax(avg_a - s, 0.0);
+          pg = a.is_call ? fmax(s - avg_g, 0.0) : fmax(avg_g - s, 0.0);
+        }
+        a.arith[i] = pa;
+        a.geo[i] = pg;
+      } else {  // kExoAsianSeasoned (floating strike)
+        const double avg_rem = a.geometric ? avg_g : avg_a;
+        const double avg_t = a.geometric ? exp(log(a.a_spent) * a.w_spent + log(avg_rem) * a.w_remain)
+                                         : a.w_spent * a.a_spent + a.w_remain * avg_rem;
+        sum += a.is_call ? fmax(s - avg_t, 0.0) : fmax(avg_t - s, 0.0);
+      }
+    }
+  }
+  if (a.kind != kExoAsian) block_sum2_store(sum, 0.0, a.partials + 2 * (uint64_t)blockIdx.x);
+  if (err) atomicOr(a.err, err);
+}
+
 }  // namespace
 
 int exotic_grid(uint64_t n, int sms) {
@@ -258,7 +350,10 @@ void launch_exotic(const ExoticLaunch& a, int grid, cudaStream_t st) {
     b.f_lb = (float)a.lbarrier;
     b.f_lm0 = (float)a.lm0;
     b.f_ln0 = (float)a.ln0;
-    k_exotic_f32<<<grid, 128, 0, st>>>(b);
+    if (a.steps < (1ull << 31))
+      k_exotic_f32<<<grid, 128, 0, st>>>(b);
+    else
+      k_exotic_f32_loop<<<grid, 128, 0, st>>>(b);
   } else
     k_exotic<<<grid, 128, 0, st>>>(a);
 }
