@@ -248,7 +248,7 @@ __global__ void k_asian_means(const double* __restrict__ totals, uint64_t n, dou
 // loop form's, so the per-thread sums and the block totals are the same bits.
 // A knocked-out barrier path stops drawing (its lane needs no more normals);
 // a knock-in path draws to maturity.
-__global__ void __launch_bounds__(128) k_exotic_f32(const __grid_constant__ ExoticLaunch a) {
+__global__ void __launch_bounds__(128, 8) k_exotic_f32(const __grid_constant__ ExoticLaunch a) {
   __shared__ ZigShared32 zs;
   zig_stage32(zs, a.tabs);
   const SamplerCtx c{a.tabs, a.tabs->r32, a.tabs->r};
