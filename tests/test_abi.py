@@ -301,6 +301,27 @@ def test_tune_table_host_logic(stocha):
                         variant=before_m3["variant"], n_assets=3)
 
 
+def test_top_layer_always_rejects(stocha):
+    """The warp-uniform FP32 sampler sends a failed attempt in the top layer
+    (L = 255) to a state that only consumes its second draw, without a wedge
+    test.  That rests on the reference's tables: the layer's fast threshold
+    is 0 (X[256] = 0, normal.rs:25-27), so every top-layer attempt leaves the
+    fast path, and its wedge test can never accept (Y[255] = Y[256] = 1, so
+    y = 1 >= exp(-x^2/2), normal.rs:38-42).  Every other layer has a positive
+    threshold."""
+    from stocha_gb300 import _lib
+    from tests.test_oracle import _table_from_inc
+
+    lib = _lib.load()
+    thr = np.zeros(256, np.uint64)
+    lib.stocha_debug_zig_thresholds.argtypes = [_lib.P_u64]
+    assert lib.stocha_debug_zig_thresholds(thr.ctypes.data_as(_lib.P_u64)) == 0
+    _, X, Y = _table_from_inc()
+    assert int(thr[255]) == 0 and X[256] == 0.0
+    assert Y[255] == 1.0 and Y[256] == 1.0
+    assert all(int(thr[L]) > 0 for L in range(255))
+
+
 def test_greeks_batch_step_limit(stocha):
     """The FP32 batch kernel counts a path's normals in 32 bits: an FP32
     instance with 2^32 steps or more is a value error before any CUDA call."""
