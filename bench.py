@@ -566,27 +566,36 @@ FP32_FUSED_NCU = {
 }
 
 
-def oracle_headline_step(cores):
+def oracle_headline_step(cores, n_paths=None):
     """One step of the headline workload on the host cores by the oracle (the
     C++ restatement of the reference's Rayon algorithm): the three models'
-    FP64 paths, each gathered serially into a new array as gbm.rs:99-105
-    does.  Returns the seconds taken."""
+    FP64 paths (n_paths each, the full 1e6 unless given), each gathered
+    serially into a new array as gbm.rs:99-105 does.  Returns the seconds
+    taken."""
     import numpy as np
 
     from oracle import oracle as O
 
+    n = N_PATHS if n_paths is None else n_paths
     corr = np.array(CORR3)
     t0 = time.perf_counter()
-    p = O.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, N_PATHS, seed=SEED, threads=cores,
+    p = O.multi_gbm(MULTI["s0"], MULTI["mu"], MULTI["sigma"], corr, 1.0, STEPS, n, seed=SEED, threads=cores,
                     gather=True)
     del p
-    p = O.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")], STEPS, N_PATHS,
+    p = O.heston(*[HESTON[k] for k in ("s0", "v0", "mu", "kappa", "theta", "xi", "rho", "t")], STEPS, n,
                  seed=SEED, threads=cores, gather=True)
     del p
-    p = O.merton(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j", "sigma_j", "t")], STEPS, N_PATHS,
+    p = O.merton(*[MERTON[k] for k in ("s0", "mu", "sigma", "lambda_", "mu_j", "sigma_j", "t")], STEPS, n,
                  seed=SEED, threads=cores, gather=True)
     del p
     return time.perf_counter() - t0
+
+
+# Seconds the reference arm's timed steps may take in all: past this, each
+# step prices the first paths of the workload only (path-steps/s is the
+# per-path rate, so the sample does not change it), so that any --steps ends
+# within a few minutes.
+REFERENCE_TIMED_BUDGET_S = 150.0
 
 
 def run_reference(args, rank, world):
@@ -600,12 +609,19 @@ def run_reference(args, rank, world):
 
     O.build()
     cores = host_cores()
-    for _ in range(args.warmup):
-        oracle_headline_step(cores)
-    times = [oracle_headline_step(cores) for _ in range(args.steps)]
+    # the warm-up steps run the full workload; the first one sizes the timed steps
+    n_step = N_PATHS
+    for w in range(args.warmup):
+        t_full = oracle_headline_step(cores)
+        if w == 0 and args.steps * t_full > REFERENCE_TIMED_BUDGET_S:
+            n_step = max(10_000, int(N_PATHS * REFERENCE_TIMED_BUDGET_S / (args.steps * t_full)) // 1000 * 1000)
+    times = [oracle_headline_step(cores, n_step) for _ in range(args.steps)]
     total = sum(times)
-    path_steps = 3 * N_PATHS * STEPS
+    path_steps = 3 * n_step * STEPS
     value = path_steps * len(times) / total
+    sample = (f"the full workload: 3 models x {N_PATHS} paths x {STEPS} steps" if n_step == N_PATHS else
+              f"the first {n_step} of the {N_PATHS} paths of each model x {STEPS} steps per step (the timed "
+              f"steps kept within {REFERENCE_TIMED_BUDGET_S:.0f} s)")
     line = {
         "impl": "reference", "metric": "path-steps/s", "value": value, "unit": "path-steps/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -613,8 +629,7 @@ def run_reference(args, rank, world):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded; reference parameters)",
         "config": headline_config(),
         "cpu_baseline": {"value": value, "unit": "path-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"the full workload: 3 models x {N_PATHS} paths x {STEPS} steps, FP64 paths "
-                                   "gathered into host arrays"},
+                         "sample": sample + ", FP64 paths gathered into host arrays"},
         "e2e": {"value": value, "unit": "path-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "C++ restatement of stocha's Rayon algorithm (the Rust reference cannot be built here)",
     }
